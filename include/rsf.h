@@ -1,0 +1,156 @@
+/*
+ * rsf.h -- C ABI of the GB300 RSF level-set library (librsf_gb300.so).
+ *
+ * Region-scalable-fitting level-set evolution of 3-D sub-volumes, as run by
+ * the `rsf3d` executable of STIM-Lab/paper-rsf-vesselseg (CUDA_RSF/main.cpp
+ * and CUDA_RSF/kernel.cu).  Plain C: pointers, sizes and status codes only.
+ *
+ * Conventions
+ *   - Volumes are dense, x fastest: element (x, y, z) of a W x H x L volume is
+ *     at z*W*H + y*W + x (the reference's indexing, CUDA_RSF/kernel.cu:73).
+ *     A NumPy array of shape (L, H, W) in C order has this layout.
+ *   - Unless a function says "host", pointers are DEVICE pointers owned by
+ *     the caller.  Nothing is allocated per call: scratch lives in an
+ *     rsf_workspace that the caller creates and destroys explicitly.
+ *   - Every call is asynchronous on the given stream (0 = legacy default
+ *     stream) and returns an rsf_status; nothing prints, nothing exits.
+ *     Errors found while kernels run are reported by rsf_workspace_check().
+ *   - A workspace may be used by one stream at a time; different workspaces
+ *     are independent and may run concurrently.
+ */
+#ifndef RSF_GB300_H
+#define RSF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSF_ABI_VERSION 1
+
+typedef enum {
+    RSF_OK = 0,
+    RSF_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad count, bad parameter */
+    RSF_ERR_SHAPE = 2,            /* extent < 2 or too large */
+    RSF_ERR_DTYPE = 3,            /* unknown rsf_dtype */
+    RSF_ERR_UNSUPPORTED = 4,      /* valid but not implemented combination */
+    RSF_ERR_NO_MEMORY = 5,        /* workspace allocation failed */
+    RSF_ERR_WORKSPACE_TOO_SMALL = 6,
+    RSF_ERR_CUDA = 7,             /* a CUDA runtime call failed */
+    RSF_ERR_NONFINITE = 8,        /* NaN/Inf appeared in phi (checked on demand) */
+    RSF_ERR_IO = 9,               /* .npy read/write (host helpers) */
+    RSF_ERR_NO_DEVICE = 10
+} rsf_status;
+
+typedef enum {
+    RSF_U8 = 0,  /* uint8 image (the 8-bit stacks the pipeline produces) */
+    RSF_F32 = 1  /* float32 image (what the reference loads, main.cpp:148) */
+} rsf_dtype;
+
+typedef enum {
+    /* x = 0 reads the previous linear element, as the reference's
+     * gradient_dx_cuda does (kernel.cu:64-67, an unsigned "j - 1 < 0" test that
+     * never fires); voxel 0 reads itself instead of element -1. */
+    RSF_BOUNDARY_REFERENCE = 0,
+    /* x = 0 uses the one-sided difference (f[1]-f[0])/2 like the y and z rules */
+    RSF_BOUNDARY_CLAMP = 1
+} rsf_boundary;
+
+typedef enum {
+    /* float-only IEEE sequences (compensated where the reference used double,
+     * own atan); bit-identical to the CPU oracle on every platform. */
+    RSF_ARITH_PORTABLE = 0,
+    /* the reference's own arithmetic: CUDA atanf and double precision at the
+     * spots kernel.cu evaluates in double.  Slow on GB300 (FP64). */
+    RSF_ARITH_REFERENCE = 1
+} rsf_arith;
+
+/* Parameters of one evolution.  Defaults (rsf_params_default) are the
+ * reference's command-line defaults, main.cpp:91-97. */
+typedef struct {
+    float sigma;    /* --sigma 5.0: Gaussian sigma of the local fit */
+    float dt;       /* --dt 0.1 */
+    float mu;       /* --meu 1.0: distance-regularisation weight */
+    float lambda1;  /* --e 0.1: weight of e_out (inside the phi > 0 region) */
+    float lambda2;  /* --e 0.1: weight of e_in */
+    float nu;       /* --v 1e-4: curvature (length) weight */
+    float eps;      /* 0.2: Heaviside/Dirac width, hard-coded in kernel.cu:258,275 */
+    float sigma2;   /* --sigma2 0.0: (int) radius of the e-term box window */
+    int32_t boundary; /* rsf_boundary */
+    int32_t arith;    /* rsf_arith */
+    int32_t reserved[6];
+} rsf_params;
+
+/* One sub-volume of a batch.  All pointers are device pointers. */
+typedef struct {
+    float *phi;        /* in/out level set, W*H*L float32 */
+    const void *image; /* W*H*L image of the batch's dtype */
+    int64_t W, H, L;
+} rsf_subvol;
+
+typedef struct rsf_workspace rsf_workspace;
+
+/* Library identification. */
+int rsf_abi_version(void);
+const char *rsf_status_string(rsf_status s);
+/* Message of the last failure on the calling thread (empty if none). */
+const char *rsf_last_error(void);
+
+/* Fills the reference defaults. */
+rsf_status rsf_params_default(rsf_params *p);
+
+/* The Gaussian taps the evolution uses for `sigma` (main.cpp:152-166:
+ * k = floor(7 sigma) made odd, g[i] = exp(-(i-k/2)^2/u)/sqrt(u pi) with
+ * u = (int)(2 sigma^2), not normalised).  Host memory; `cap` entries. */
+rsf_status rsf_gaussian_taps(float sigma, float *taps_host, int cap, int *k_out);
+
+/* Workspace sized for batches of up to `max_voxels` voxels in total (summed
+ * over sub-volumes) and up to `max_subvols` sub-volumes.  Allocates device
+ * memory on the current device. */
+rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_workspace **ws);
+rsf_status rsf_workspace_destroy(rsf_workspace *ws);
+/* Bytes of device memory the workspace holds. */
+size_t rsf_workspace_bytes(const rsf_workspace *ws);
+/* Device bytes a workspace for `max_voxels` / `max_subvols` would hold. */
+size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols);
+
+/* Evolves one volume in place for `iters` iterations: the device-resident
+ * equivalent of the reference's hot loop (main.cpp:222-314).
+ * Replaces the per-op host wrappers declared at main.cpp:56-71. */
+rsf_status rsf_evolve(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
+                      float *phi, int64_t W, int64_t H, int64_t L, int32_t iters, void *stream);
+
+/* Evolves `n` independent sub-volumes of (possibly) different shapes in one
+ * launch sequence per iteration, the iteration loop captured once into a
+ * CUDA graph and replayed.  Replaces the one-process-per-sub-volume batch
+ * driver described at README.md:56 (rsfbatch.py, not in the reference). */
+rsf_status rsf_evolve_batched(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype,
+                              const rsf_subvol *subvols, int32_t n, int32_t iters, void *stream);
+
+/* Host-buffer convenience: copies image and phi to the device, evolves,
+ * copies phi back (synchronous).  `phi_host` is updated in place.  This is
+ * the call shape of the reference's wrappers (host pointers in and out). */
+rsf_status rsf_evolve_host(rsf_workspace *ws, const rsf_params *p, const void *image_host,
+                           rsf_dtype dtype, float *phi_host, int64_t W, int64_t H, int64_t L,
+                           int32_t iters);
+
+/* One iteration with the intermediate fields written out, for parity
+ * checks.  `fields` receives 8 W*H*L float32 volumes in this order:
+ * f_out, f_in, e_out, e_in, delta, kappa, laplacian, |grad phi|
+ * (the reference's fout_x, fin_x, Eout, Ein, derivative_heaviside,
+ * normalized_DIV, DIV, Gradientmagnitude_phi; main.cpp:195-211).
+ * phi_out receives the updated level set; phi is not modified. */
+rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *image,
+                          rsf_dtype dtype, const float *phi, float *phi_out, float *fields,
+                          int64_t W, int64_t H, int64_t L, void *stream);
+
+/* Waits for the workspace's stream work and reports kernel-side errors
+ * (non-finite phi when checking is enabled, CUDA launch errors). */
+rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSF_GB300_H */

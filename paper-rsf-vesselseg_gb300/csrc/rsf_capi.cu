@@ -1,0 +1,448 @@
+// rsf_capi.cu -- the extern "C" boundary declared in include/rsf.h.
+//
+// Replaces the reference's host layer: the per-op wrappers of
+// CUDA_RSF/kernel.cu (each a cudaMalloc / cudaMemcpy / launch / cudaMemcpy /
+// cudaFree bracket, forward-declared at CUDA_RSF/main.cpp:56-71) and the
+// iteration loop of CUDA_RSF/main.cpp:222-314.  Here the state stays resident
+// in device memory, scratch lives in a caller-owned workspace, and a batch of
+// sub-volumes advances one iteration per three kernel launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "rsf.h"
+#include "rsf_internal.h"
+
+using rsf::StepConst;
+using rsf::SubVolDev;
+
+namespace {
+thread_local char g_last_error[512] = "";
+
+rsf_status cuda_fail(cudaError_t e, const char *what) {
+    std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
+    return RSF_ERR_CUDA;
+}
+
+rsf_status fail(rsf_status s, const char *msg) {
+    std::snprintf(g_last_error, sizeof g_last_error, "%s", msg);
+    return s;
+}
+
+constexpr int64_t kMaxExtent = 1 << 20;
+}  // namespace
+
+struct rsf_workspace {
+    int device = -1;
+    int64_t max_voxels = 0;
+    int32_t max_subvols = 0;
+    float *pool_phi2 = nullptr;  // second level-set buffer, max_voxels
+    float *pool_x = nullptr;     // x-pass fields, 4 * max_voxels
+    float *pool_y = nullptr;     // y-pass fields, 4 * max_voxels
+    SubVolDev *d_svs = nullptr;
+    int *d_pre = nullptr;        // 3 * (max_subvols + 1)
+    unsigned *d_flag = nullptr;
+    SubVolDev *h_svs = nullptr;  // pinned staging of the table
+    int *h_pre = nullptr;
+    cudaEvent_t table_ev = nullptr;
+    bool table_pending = false;
+    cudaStream_t capture_stream = nullptr;
+    size_t bytes = 0;
+    // host-buffer convenience path (allocated on first use)
+    void *stage_img = nullptr;
+    float *stage_phi = nullptr;
+    size_t stage_voxels = 0;
+};
+
+extern "C" {
+
+int rsf_abi_version(void) { return RSF_ABI_VERSION; }
+
+const char *rsf_last_error(void) { return g_last_error; }
+
+const char *rsf_status_string(rsf_status s) {
+    switch (s) {
+        case RSF_OK: return "ok";
+        case RSF_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case RSF_ERR_SHAPE: return "invalid volume shape";
+        case RSF_ERR_DTYPE: return "unsupported image dtype";
+        case RSF_ERR_UNSUPPORTED: return "unsupported parameter combination";
+        case RSF_ERR_NO_MEMORY: return "device memory allocation failed";
+        case RSF_ERR_WORKSPACE_TOO_SMALL: return "workspace too small for this batch";
+        case RSF_ERR_CUDA: return "CUDA runtime error";
+        case RSF_ERR_NONFINITE: return "non-finite value in the level set";
+        case RSF_ERR_IO: return "file input/output error";
+        case RSF_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+rsf_status rsf_params_default(rsf_params *p) {
+    if (!p) return fail(RSF_ERR_INVALID_ARGUMENT, "params is null");
+    std::memset(p, 0, sizeof *p);
+    p->sigma = 5.0f;
+    p->dt = 0.1f;
+    p->mu = 1.0f;
+    p->lambda1 = 0.1f;
+    p->lambda2 = 0.1f;
+    p->nu = 0.0001f;
+    p->eps = 0.2f;
+    p->sigma2 = 0.0f;
+    p->boundary = RSF_BOUNDARY_REFERENCE;
+    p->arith = RSF_ARITH_PORTABLE;
+    return RSF_OK;
+}
+
+// CUDA_RSF/main.cpp:152-166.  exp is evaluated in double and rounded so that
+// the taps are the same on every host.
+rsf_status rsf_gaussian_taps(float sigma, float *taps, int cap, int *k_out) {
+    if (!(sigma > 0.0f) || !std::isfinite(sigma)) return fail(RSF_ERR_INVALID_ARGUMENT, "sigma must be > 0");
+    const float p7 = 7.0f * sigma;
+    if (p7 > (float)(rsf::MAXK)) return fail(RSF_ERR_UNSUPPORTED, "sigma too large (more than 128 taps)");
+    unsigned p = (unsigned)p7;
+    if (p % 2u == 0u) p++;
+    const float miu = (float)(p / 2u);
+    const int u = (int)(2.0f * sigma * sigma);
+    if (u < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "sigma too small: (int)(2 sigma^2) must be >= 1");
+    if ((int)p > rsf::MAXK) return fail(RSF_ERR_UNSUPPORTED, "more than 128 taps");
+    if (k_out) *k_out = (int)p;
+    if (!taps) return RSF_OK;
+    if (cap < (int)p) return fail(RSF_ERR_INVALID_ARGUMENT, "taps buffer too small");
+    const float s = std::sqrt((float)u * (float)3.14159265358979323846);
+    for (unsigned xi = 0; xi < p; xi++) {
+        const float d = (float)(int)xi - miu;
+        const float a = (-d * d) / (float)u;
+        taps[xi] = (1.0f / s) * (float)std::exp((double)a);
+    }
+    return RSF_OK;
+}
+
+size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols) {
+    const size_t v = (size_t)std::max<int64_t>(max_voxels, 0);
+    const size_t n = (size_t)std::max<int32_t>(max_subvols, 1);
+    return v * sizeof(float) * 9 + n * sizeof(SubVolDev) + 3 * (n + 1) * sizeof(int) + 256;
+}
+
+static void ws_free(rsf_workspace *ws) {
+    if (!ws) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (ws->device >= 0) cudaSetDevice(ws->device);
+    if (ws->table_ev) cudaEventSynchronize(ws->table_ev);
+    cudaFree(ws->pool_phi2);
+    cudaFree(ws->pool_x);
+    cudaFree(ws->pool_y);
+    cudaFree(ws->d_svs);
+    cudaFree(ws->d_pre);
+    cudaFree(ws->d_flag);
+    cudaFree(ws->stage_img);
+    cudaFree(ws->stage_phi);
+    cudaFreeHost(ws->h_svs);
+    cudaFreeHost(ws->h_pre);
+    if (ws->table_ev) cudaEventDestroy(ws->table_ev);
+    if (ws->capture_stream) cudaStreamDestroy(ws->capture_stream);
+    if (cur >= 0) cudaSetDevice(cur);
+    delete ws;
+}
+
+rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_workspace **out) {
+    if (!out) return fail(RSF_ERR_INVALID_ARGUMENT, "output pointer is null");
+    *out = nullptr;
+    if (max_voxels < 1 || max_subvols < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "max_voxels and max_subvols must be >= 1");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(RSF_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    rsf_workspace *ws = new rsf_workspace;
+    cudaGetDevice(&ws->device);
+    ws->max_voxels = max_voxels;
+    ws->max_subvols = max_subvols;
+    const size_t v = (size_t)max_voxels;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void **)&ws->pool_phi2, v * sizeof(float));
+    alloc((void **)&ws->pool_x, 4 * v * sizeof(float));
+    alloc((void **)&ws->pool_y, 4 * v * sizeof(float));
+    alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
+    alloc((void **)&ws->d_pre, 3 * ((size_t)max_subvols + 1) * sizeof(int));
+    alloc((void **)&ws->d_flag, 256);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, (size_t)max_subvols * sizeof(SubVolDev));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_pre, 3 * ((size_t)max_subvols + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws->table_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemset(ws->d_flag, 0, 256);
+    if (e == cudaSuccess) e = rsf::configure_device();
+    if (e != cudaSuccess) {
+        const bool oom = e == cudaErrorMemoryAllocation;
+        cudaGetLastError();
+        ws_free(ws);
+        return oom ? fail(RSF_ERR_NO_MEMORY, "workspace allocation failed") : cuda_fail(e, "workspace create");
+    }
+    ws->bytes = rsf_workspace_bytes_for(max_voxels, max_subvols);
+    *out = ws;
+    return RSF_OK;
+}
+
+rsf_status rsf_workspace_destroy(rsf_workspace *ws) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    ws_free(ws);
+    return RSF_OK;
+}
+
+size_t rsf_workspace_bytes(const rsf_workspace *ws) { return ws ? ws->bytes : 0; }
+
+}  // extern "C"
+
+namespace {
+
+rsf_status check_params(const rsf_params *p, int *k, float *taps) {
+    if (!p) return fail(RSF_ERR_INVALID_ARGUMENT, "params is null");
+    const float vals[] = {p->sigma, p->dt, p->mu, p->lambda1, p->lambda2, p->nu, p->eps, p->sigma2};
+    for (float v : vals)
+        if (!std::isfinite(v)) return fail(RSF_ERR_INVALID_ARGUMENT, "non-finite parameter");
+    if (!(p->eps > 0.0f)) return fail(RSF_ERR_INVALID_ARGUMENT, "eps must be > 0");
+    if (p->sigma2 < 0.0f) return fail(RSF_ERR_INVALID_ARGUMENT, "sigma2 must be >= 0");
+    if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "box e-term (sigma2 >= 1) is not implemented on the GPU");
+    if (p->boundary != RSF_BOUNDARY_REFERENCE && p->boundary != RSF_BOUNDARY_CLAMP)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "unknown boundary mode");
+    if (p->arith != RSF_ARITH_PORTABLE && p->arith != RSF_ARITH_REFERENCE)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
+    return rsf_gaussian_taps(p->sigma, taps, rsf::MAXK, k);
+}
+
+rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
+    if (W < 2 || H < 2 || L < 2) return fail(RSF_ERR_SHAPE, "every extent must be >= 2");
+    if (W > kMaxExtent || H > kMaxExtent || L > kMaxExtent) return fail(RSF_ERR_SHAPE, "extent too large");
+    if ((double)W * (double)H * (double)L > 1.0e12) return fail(RSF_ERR_SHAPE, "volume too large");
+    return RSF_OK;
+}
+
+// Lays out a batch in the workspace pools and uploads the table.
+rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, rsf_dtype dtype,
+                   const float *const *phi_out_override, int totals[3], cudaStream_t st) {
+    if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
+    if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
+    if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
+    int64_t total = 0;
+    for (int i = 0; i < n; i++) {
+        if (!svs[i].phi || !svs[i].image) return fail(RSF_ERR_INVALID_ARGUMENT, "null sub-volume pointer");
+        rsf_status s = check_shape(svs[i].W, svs[i].H, svs[i].L);
+        if (s != RSF_OK) return s;
+        total += svs[i].W * svs[i].H * svs[i].L;
+    }
+    if (total > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "batch larger than the workspace");
+    if (ws->table_pending) {
+        cudaError_t e = cudaEventSynchronize(ws->table_ev);
+        if (e != cudaSuccess) return cuda_fail(e, "table event");
+        ws->table_pending = false;
+    }
+    const int n1 = n + 1;
+    int *pre = ws->h_pre;
+    pre[0] = pre[n1] = pre[2 * n1] = 0;
+    size_t off_v = 0, off_x = 0, off_y = 0;
+    for (int i = 0; i < n; i++) {
+        SubVolDev d;
+        std::memset(&d, 0, sizeof d);
+        d.W = (int)svs[i].W;
+        d.H = (int)svs[i].H;
+        d.L = (int)svs[i].L;
+        rsf::tile_counts(d.W, d.H, d.L, k, d.tiles, d.Wv, d.Hv, d.Lv);
+        const size_t nv = (size_t)d.W * d.H * d.L;
+        d.phi[0] = svs[i].phi;
+        d.phi[1] = phi_out_override ? const_cast<float *>(phi_out_override[i]) : ws->pool_phi2 + off_v;
+        d.img = svs[i].image;
+        d.xb = ws->pool_x + off_x;
+        d.yb = ws->pool_y + off_y;
+        off_v += nv;
+        off_x += 4 * (size_t)d.Wv * d.H * d.L;
+        off_y += 4 * (size_t)d.Wv * d.Hv * d.L;
+        for (int j = 0; j < 3; j++) {
+            const int64_t next = (int64_t)pre[j * n1 + i] + d.tiles[j];
+            if (next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");
+            pre[j * n1 + i + 1] = (int)next;
+        }
+        ws->h_svs[i] = d;
+    }
+    for (int j = 0; j < 3; j++) totals[j] = pre[j * n1 + n];
+    cudaError_t e = cudaMemcpyAsync(ws->d_svs, ws->h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ws->d_pre, ws->h_pre, 3 * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ws->table_ev, st);
+    if (e != cudaSuccess) return cuda_fail(e, "table upload");
+    ws->table_pending = true;
+    return RSF_OK;
+}
+
+StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n) {
+    StepConst c;
+    std::memset(&c, 0, sizeof c);
+    for (int i = 0; i < k; i++) c.taps[i] = taps[i];
+    c.k = k;
+    c.r = (k - 1) / 2;
+    c.eps = p->eps;
+    c.dt = p->dt;
+    c.mu = p->mu;
+    c.nu = p->nu;
+    c.l1 = p->lambda1;
+    c.l2 = p->lambda2;
+    c.lam_equal = p->lambda1 == p->lambda2;
+    c.boundary = p->boundary;
+    c.img_f32 = dtype == RSF_F32;
+    c.nsv = n;
+    return c;
+}
+
+// Copies the second buffer back into the caller's phi after an odd number
+// of iterations.
+rsf_status copy_back(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, cudaStream_t st) {
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        const size_t nv = (size_t)svs[i].W * svs[i].H * svs[i].L;
+        cudaError_t e = cudaMemcpyAsync(svs[i].phi, ws->pool_phi2 + off, nv * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "copy back");
+        off += nv;
+    }
+    return RSF_OK;
+}
+
+rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rsf_subvol *svs, int32_t n,
+               int32_t iters, cudaStream_t st, bool use_graph) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    if (iters < 0) return fail(RSF_ERR_INVALID_ARGUMENT, "iters must be >= 0");
+    float taps[rsf::MAXK];
+    int k = 0;
+    rsf_status s = check_params(p, &k, taps);
+    if (s != RSF_OK) return s;
+    int tot[3];
+    s = prepare(ws, svs, n, k, dtype, nullptr, tot, st);
+    if (s != RSF_OK) return s;
+    if (iters == 0) return RSF_OK;
+    const StepConst c = make_const(p, k, taps, dtype, n);
+    cudaError_t e = cudaSuccess;
+    if (!use_graph) {
+        for (int it = 0; it < iters && e == cudaSuccess; it++)
+            e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, it & 1, p->arith, ws->d_flag, nullptr, st);
+        if (e != cudaSuccess) return cuda_fail(e, "step launch");
+    } else {
+        // Capture two iterations (phi -> phi2 -> phi) once, replay them.
+        auto capture = [&](int count, cudaGraphExec_t *exec) -> cudaError_t {
+            cudaGraph_t g = nullptr;
+            cudaError_t err = cudaStreamBeginCapture(ws->capture_stream, cudaStreamCaptureModeThreadLocal);
+            if (err != cudaSuccess) return err;
+            for (int it = 0; it < count && err == cudaSuccess; it++)
+                err = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, it & 1, p->arith, ws->d_flag, nullptr,
+                                       ws->capture_stream);
+            cudaError_t end = cudaStreamEndCapture(ws->capture_stream, &g);
+            if (err == cudaSuccess) err = end;
+            if (err == cudaSuccess) err = cudaGraphInstantiate(exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            return err;
+        };
+        cudaGraphExec_t pair = nullptr, single = nullptr;
+        if (iters >= 2) e = capture(2, &pair);
+        if (e == cudaSuccess && (iters & 1)) e = capture(1, &single);
+        for (int i = 0; i < iters / 2 && e == cudaSuccess; i++) e = cudaGraphLaunch(pair, st);
+        if (e == cudaSuccess && single) e = cudaGraphLaunch(single, st);
+        if (pair) cudaGraphExecDestroy(pair);
+        if (single) cudaGraphExecDestroy(single);
+        if (e != cudaSuccess) return cuda_fail(e, "graph");
+    }
+    if (iters & 1) return copy_back(ws, svs, n, st);
+    return RSF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rsf_status rsf_evolve(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype, float *phi,
+                      int64_t W, int64_t H, int64_t L, int32_t iters, void *stream) {
+    rsf_subvol sv = {phi, image, W, H, L};
+    return run(ws, p, dtype, &sv, 1, iters, (cudaStream_t)stream, false);
+}
+
+rsf_status rsf_evolve_batched(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rsf_subvol *subvols,
+                              int32_t n, int32_t iters, void *stream) {
+    if (!subvols) return fail(RSF_ERR_INVALID_ARGUMENT, "subvols is null");
+    return run(ws, p, dtype, subvols, n, iters, (cudaStream_t)stream, true);
+}
+
+rsf_status rsf_evolve_host(rsf_workspace *ws, const rsf_params *p, const void *image_host, rsf_dtype dtype,
+                           float *phi_host, int64_t W, int64_t H, int64_t L, int32_t iters) {
+    if (!ws || !image_host || !phi_host) return fail(RSF_ERR_INVALID_ARGUMENT, "null argument");
+    rsf_status s = check_shape(W, H, L);
+    if (s != RSF_OK) return s;
+    if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
+    const size_t nv = (size_t)W * H * L;
+    if ((int64_t)nv > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "volume larger than the workspace");
+    if (ws->stage_voxels < nv) {
+        cudaFree(ws->stage_img);
+        cudaFree(ws->stage_phi);
+        ws->stage_img = nullptr;
+        ws->stage_phi = nullptr;
+        ws->stage_voxels = 0;
+        cudaError_t e = cudaMalloc(&ws->stage_img, nv * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&ws->stage_phi, nv * sizeof(float));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(RSF_ERR_NO_MEMORY, "staging allocation failed");
+        }
+        ws->stage_voxels = nv;
+    }
+    const size_t ib = nv * (dtype == RSF_F32 ? 4 : 1);
+    cudaStream_t st = ws->capture_stream;
+    cudaError_t e = cudaMemcpyAsync(ws->stage_img, image_host, ib, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws->stage_phi, phi_host, nv * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "host to device");
+    rsf_subvol sv = {ws->stage_phi, ws->stage_img, W, H, L};
+    s = run(ws, p, dtype, &sv, 1, iters, st, false);
+    if (s != RSF_OK) return s;
+    e = cudaMemcpyAsync(phi_host, ws->stage_phi, nv * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "device to host");
+    return RSF_OK;
+}
+
+rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
+                          const float *phi, float *phi_out, float *fields, int64_t W, int64_t H, int64_t L,
+                          void *stream) {
+    if (!ws || !phi || !phi_out || !fields || !image) return fail(RSF_ERR_INVALID_ARGUMENT, "null argument");
+    float taps[rsf::MAXK];
+    int k = 0;
+    rsf_status s = check_params(p, &k, taps);
+    if (s != RSF_OK) return s;
+    rsf_subvol sv = {const_cast<float *>(phi), image, W, H, L};
+    const float *outs[1] = {phi_out};
+    int tot[3];
+    cudaStream_t st = (cudaStream_t)stream;
+    s = prepare(ws, &sv, 1, k, dtype, outs, tot, st);
+    if (s != RSF_OK) return s;
+    const StepConst c = make_const(p, k, taps, dtype, 1);
+    const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};
+    cudaError_t e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, 0, p->arith, ws->d_flag, &dbg, st);
+    return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");
+}
+
+rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "stream");
+    unsigned flag = 0;
+    e = cudaMemcpy(&flag, ws->d_flag, sizeof flag, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && flag) e = cudaMemset(ws->d_flag, 0, sizeof flag);
+    if (e != cudaSuccess) return cuda_fail(e, "flag read");
+    if (flag) return fail(RSF_ERR_NONFINITE, "non-finite value written to phi");
+    return RSF_OK;
+}
+
+}  // extern "C"

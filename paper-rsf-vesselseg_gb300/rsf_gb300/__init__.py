@@ -1,0 +1,8 @@
+"""GB300-native RSF (region-scalable fitting) level-set evolution.
+
+The evolution runs in librsf_gb300.so (hand-written sm_103a CUDA behind the C
+ABI of include/rsf.h); this package is its Python face.
+"""
+from .api import Params, Workspace, gaussian_taps  # noqa: F401
+
+__all__ = ["Params", "Workspace", "gaussian_taps"]

@@ -1,0 +1,173 @@
+"""Python face of the C ABI: parameters with the reference's flag names and
+evolution entry points over torch CUDA tensors or NumPy host arrays.
+
+The reference's executable takes --sigma --t --dt --meu --e --v --sigma2
+(CUDA_RSF/main.cpp:88-102); `Params` keeps those meanings (and defaults) and
+adds the knobs the reference hard-codes: eps (kernel.cu:258,275), separate
+lambda1/lambda2, the x = 0 boundary rule and the arithmetic definition.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import RsfParams, RsfSubvol, check
+
+
+@dataclass
+class Params:
+    sigma: float = 5.0      # --sigma
+    dt: float = 0.1         # --dt
+    mu: float = 1.0         # --meu
+    lambda1: float = 0.1    # --e (weight of e_out)
+    lambda2: float = 0.1    # --e (weight of e_in)
+    nu: float = 0.0001      # --v
+    eps: float = 0.2        # hard-coded in the reference
+    sigma2: float = 0.0     # --sigma2
+    boundary: str = "reference"  # or "clamp"
+    arith: str = "portable"      # or "reference"
+
+    def to_c(self) -> RsfParams:
+        p = RsfParams()
+        p.sigma, p.dt, p.mu = self.sigma, self.dt, self.mu
+        p.lambda1, p.lambda2, p.nu = self.lambda1, self.lambda2, self.nu
+        p.eps, p.sigma2 = self.eps, self.sigma2
+        p.boundary = {"reference": 0, "clamp": 1}[self.boundary]
+        p.arith = {"portable": 0, "reference": 1}[self.arith]
+        return p
+
+    @classmethod
+    def from_flags(cls, sigma=5.0, t=None, dt=0.1, meu=1.0, e=0.1, v=0.0001, sigma2=0.0, **kw):
+        """Builds Params from the reference's flag names (`t` is ignored here)."""
+        return cls(sigma=sigma, dt=dt, mu=meu, lambda1=e, lambda2=e, nu=v, sigma2=sigma2, **kw)
+
+
+def gaussian_taps(sigma: float) -> np.ndarray:
+    lib = _lib.load()
+    k = ctypes.c_int(0)
+    check(lib.rsf_gaussian_taps(ctypes.c_float(sigma), None, 0, ctypes.byref(k)))
+    buf = (ctypes.c_float * k.value)()
+    check(lib.rsf_gaussian_taps(ctypes.c_float(sigma), buf, k.value, ctypes.byref(k)))
+    return np.frombuffer(buf, dtype=np.float32).copy()
+
+
+def _dtype_code(dt) -> int:
+    s = str(dt)
+    if s in ("uint8", "torch.uint8"):
+        return _lib.RSF_U8
+    if s in ("float32", "torch.float32"):
+        return _lib.RSF_F32
+    raise TypeError(f"image dtype must be uint8 or float32, got {s}")
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class Workspace:
+    """Device scratch for batches of up to `max_voxels` voxels in total."""
+
+    def __init__(self, max_voxels: int, max_subvols: int = 1):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.rsf_workspace_create(int(max_voxels), int(max_subvols), ctypes.byref(h)))
+        self.handle = h
+        self.max_voxels = int(max_voxels)
+        self.max_subvols = int(max_subvols)
+
+    @property
+    def nbytes(self) -> int:
+        return int(self._lib.rsf_workspace_bytes(self.handle))
+
+    def close(self):
+        if self.handle:
+            check(self._lib.rsf_workspace_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def check(self, stream=None):
+        check(self._lib.rsf_workspace_check(self.handle, ctypes.c_void_p(_stream_ptr(stream))))
+
+    # ---- device tensors -------------------------------------------------
+    def evolve(self, image, phi, params: Params, iters: int, stream=None):
+        """Evolves torch CUDA tensor `phi` (float32, shape (L, H, W)) in place."""
+        _require_cuda(image, phi)
+        L, H, W = phi.shape
+        check(self._lib.rsf_evolve(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image.data_ptr()),
+                                   _dtype_code(image.dtype), ctypes.c_void_p(phi.data_ptr()), W, H, L, int(iters),
+                                   ctypes.c_void_p(_stream_ptr(stream))))
+        return phi
+
+    def evolve_batched(self, pairs, params: Params, iters: int, stream=None):
+        """Evolves a list of (image, phi) CUDA tensor pairs, each phi in place."""
+        if not pairs:
+            raise ValueError("empty batch")
+        codes = {_dtype_code(img.dtype) for img, _ in pairs}
+        if len(codes) != 1:
+            raise TypeError("all images of a batch must share one dtype")
+        arr = (RsfSubvol * len(pairs))()
+        for i, (img, phi) in enumerate(pairs):
+            _require_cuda(img, phi)
+            L, H, W = phi.shape
+            arr[i] = RsfSubvol(phi.data_ptr(), img.data_ptr(), W, H, L)
+        check(self._lib.rsf_evolve_batched(self.handle, ctypes.byref(params.to_c()), codes.pop(), arr, len(pairs),
+                                           int(iters), ctypes.c_void_p(_stream_ptr(stream))))
+        return [phi for _, phi in pairs]
+
+    def step_debug(self, image, phi, params: Params, stream=None):
+        """One iteration; returns (phi_out, fields[8]) as new CUDA tensors."""
+        import torch
+        _require_cuda(image, phi)
+        L, H, W = phi.shape
+        out = torch.empty_like(phi)
+        fields = torch.empty((8, L, H, W), dtype=torch.float32, device=phi.device)
+        check(self._lib.rsf_step_debug(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image.data_ptr()),
+                                       _dtype_code(image.dtype), ctypes.c_void_p(phi.data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(fields.data_ptr()), W, H, L,
+                                       ctypes.c_void_p(_stream_ptr(stream))))
+        return out, fields
+
+    # ---- host arrays ----------------------------------------------------
+    def evolve_host(self, image: np.ndarray, phi: np.ndarray, params: Params, iters: int) -> np.ndarray:
+        """Host-buffer call shape of the reference: copies in, evolves, copies
+        back.  `phi` (float32, C order) is updated in place and returned."""
+        if phi.dtype != np.float32 or not phi.flags.c_contiguous:
+            raise TypeError("phi must be a C-contiguous float32 array")
+        if image.shape != phi.shape or not image.flags.c_contiguous:
+            raise TypeError("image must be C-contiguous with phi's shape")
+        L, H, W = phi.shape
+        check(self._lib.rsf_evolve_host(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image.ctypes.data),
+                                        _dtype_code(image.dtype), ctypes.c_void_p(phi.ctypes.data), W, H, L,
+                                        int(iters)))
+        return phi
+
+    def evolve_host_ptr(self, image_ptr: int, image_dtype, phi_ptr: int, shape, params: Params, iters: int):
+        """Same as evolve_host for raw host pointers (e.g. pinned torch tensors)."""
+        L, H, W = shape
+        check(self._lib.rsf_evolve_host(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image_ptr),
+                                        _dtype_code(image_dtype), ctypes.c_void_p(phi_ptr), W, H, L, int(iters)))
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if not getattr(t, "is_cuda", False):
+            raise TypeError("expected CUDA tensors")
+        if not t.is_contiguous():
+            raise TypeError("expected contiguous tensors")

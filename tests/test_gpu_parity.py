@@ -1,0 +1,142 @@
+"""GPU parity: the CUDA path against the CPU oracle, through the C ABI.
+
+The portable arithmetic of the CUDA kernels performs the oracle's exact IEEE
+operation sequence, so the bar is bit equality of every voxel (tolerance 0),
+which also meets max|dphi| <= 1e-4 max|phi| and >= 99.99% sign agreement.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(shape, seed, dtype="u8", n_tubes=3):
+    from rsf_gb300 import synth
+
+    img, phi0, mask = synth.make_small(shape, n_tubes=n_tubes, r_min=1.5, r_max=3.5, seed=seed)
+    if phi0.min() >= 0 or phi0.max() <= 0:
+        # too thin for a tube to survive the perturbation: use a random contour
+        phi0 = np.random.default_rng(seed).uniform(-3.0, 3.0, size=shape).astype(np.float32)
+    if dtype == "f32":
+        img = img.astype(np.float32)
+    return img, phi0, mask
+
+
+def _oracle_params(orc, p):
+    return orc.params(sigma=p.sigma, dt=p.dt, mu=p.mu, lambda1=p.lambda1, lambda2=p.lambda2, nu=p.nu, eps=p.eps,
+                      boundary=0 if p.boundary == "reference" else 1)
+
+
+def _bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+
+
+def _diff_report(got, want):
+    d = np.abs(got.astype(np.float64) - want)
+    return (f"{int((got != want).sum())} voxels differ, max|d|={d.max():.3g}, "
+            f"first at {np.unravel_index(int(np.argmax(got != want)), got.shape)}")
+
+
+CASES = [
+    # shape (L, H, W), sigma, eps, lambda1, lambda2, boundary, dtype, iters
+    ((20, 26, 30), 1.5, 1.0, 1.0, 1.0, "reference", "u8", 3),      # k = 11, generic-k kernels
+    ((40, 44, 48), 3.0, 0.2, 1.0, 1.0, "reference", "u8", 2),      # k = 21 specialisation
+    ((40, 36, 50), 3.0, 1.0, 1.0, 2.0, "clamp", "f32", 2),         # lambda1 != lambda2, clamp rule
+    ((64, 40, 38), 5.0, 0.2, 0.1, 0.1, "reference", "u8", 2),      # k = 35, reference defaults
+    ((33, 45, 37), 4.0, 0.2, 1.0, 1.0, "reference", "u8", 2),      # k = 29 (even floor(7 sigma))
+    ((9, 12, 10), 3.0, 0.2, 1.0, 1.0, "reference", "u8", 3),       # smaller than the kernel: all border
+    ((17, 2, 5), 1.0, 0.2, 1.0, 1.0, "reference", "f32", 4),       # two-voxel extent
+    ((3, 70, 2), 1.0, 0.2, 1.0, 1.0, "clamp", "u8", 2),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-s{c[1]}-e{c[2]}-{c[5]}-{c[6]}")
+def test_evolve_bit_exact(case, orc, ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params
+
+    shape, sigma, eps, l1, l2, boundary, dtype, iters = case
+    img, phi0, _ = _inputs(shape, seed=hash(shape) % 1000, dtype=dtype)
+    p = Params(sigma=sigma, dt=0.1, mu=1.0, lambda1=l1, lambda2=l2, nu=65.025, eps=eps, boundary=boundary)
+    ti = torch.from_numpy(img).to(cuda)
+    tp = torch.from_numpy(phi0).to(cuda)
+    ws_big.evolve(ti, tp, p, iters)
+    ws_big.check()
+    got = tp.cpu().numpy()
+    want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), iters)
+    assert _bits_equal(got, want), _diff_report(got, want)
+
+
+@pytest.mark.parametrize("sigma,boundary", [(3.0, "reference"), (1.5, "clamp"), (5.0, "reference")])
+def test_debug_fields_bit_exact(sigma, boundary, orc, ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params
+
+    img, phi0, _ = _inputs((44, 41, 47), seed=3)
+    p = Params(sigma=sigma, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=0.2, boundary=boundary)
+    out, fields = ws_big.step_debug(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda), p)
+    torch.cuda.synchronize()
+    want_out, want_fields = orc.step(phi0, img.astype(np.float32), _oracle_params(orc, p), debug=True)
+    names = ["f_out", "f_in", "e_out", "e_in", "delta", "kappa", "laplacian", "|grad|"]
+    got_fields = fields.cpu().numpy()
+    for i, n in enumerate(names):
+        assert _bits_equal(got_fields[i], want_fields[i]), f"{n}: {_diff_report(got_fields[i], want_fields[i])}"
+    assert _bits_equal(out.cpu().numpy(), want_out)
+
+
+def test_batched_matches_plain(ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params
+
+    shapes = [(30, 40, 50), (64, 33, 29), (25, 25, 25), (12, 70, 41), (9, 9, 9)]
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=1.0)
+    pairs, plain = [], []
+    for i, s in enumerate(shapes):
+        img, phi0, _ = _inputs(s, seed=10 + i)
+        ti = torch.from_numpy(img).to(cuda)
+        pairs.append((ti, torch.from_numpy(phi0).to(cuda)))
+        tp = torch.from_numpy(phi0).to(cuda)
+        ws_big.evolve(ti, tp, p, 5)
+        plain.append(tp)
+    ws_big.evolve_batched(pairs, p, 5)
+    ws_big.check()
+    for (_, b), a in zip(pairs, plain):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("eps", [1.0, 0.2])
+def test_config0_full_evolution_bit_exact(eps, orc, ws_big, cuda):
+    """128^3 volume, 12 tubes, sigma 3, lambda 1, mu 1, nu 0.001*255^2, dt 0.1, 100 iterations."""
+    import torch
+    from rsf_gb300 import Params, synth
+
+    img, phi0, mask = synth.make_volume(synth.CONFIG0)
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=0.001 * 255 ** 2, eps=eps)
+    tp = torch.from_numpy(phi0).to(cuda)
+    ws_big.evolve(torch.from_numpy(img).to(cuda), tp, p, 100)
+    ws_big.check()
+    got = tp.cpu().numpy()
+    want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), 100)
+    maxphi = float(np.abs(want).max())
+    assert float(np.abs(got - want).max()) <= 1e-4 * maxphi
+    assert float((np.sign(got) == np.sign(want)).mean()) >= 0.9999
+    assert _bits_equal(got, want), _diff_report(got, want)
+
+
+def test_reference_arith_close_to_portable(ws_big, cuda):
+    """RSF_ARITH_REFERENCE (CUDA atanf, double spots) differs from the portable
+    definition by at most a few ulp per stage after one iteration."""
+    import torch
+    from rsf_gb300 import Params
+
+    img, phi0, _ = _inputs((40, 44, 48), seed=5)
+    ti = torch.from_numpy(img).to(cuda)
+    outs = []
+    for arith in ("portable", "reference"):
+        p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=0.2, arith=arith)
+        tp = torch.from_numpy(phi0).to(cuda)
+        ws_big.evolve(ti, tp, p, 1)
+        outs.append(tp.cpu().numpy())
+    a, b = outs
+    assert float((np.sign(a) == np.sign(b)).mean()) >= 0.9999
+    assert float(np.abs(a - b).max()) <= 1e-3 * float(np.abs(a).max())
