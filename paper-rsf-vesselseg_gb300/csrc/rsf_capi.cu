@@ -45,7 +45,7 @@ struct rsf_workspace {
     float *pool_x = nullptr;     // x-pass fields, 4 * max_voxels
     float *pool_y = nullptr;     // y-pass fields, 4 * max_voxels
     SubVolDev *d_svs = nullptr;
-    int *d_pre = nullptr;        // 3 * (max_subvols + 1)
+    int *d_pre = nullptr;        // NKERN * (max_subvols + 1)
     unsigned *d_flag = nullptr;
     SubVolDev *h_svs = nullptr;  // pinned staging of the table
     int *h_pre = nullptr;
@@ -125,7 +125,7 @@ rsf_status rsf_gaussian_taps(float sigma, float *taps, int cap, int *k_out) {
 size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols) {
     const size_t v = (size_t)std::max<int64_t>(max_voxels, 0);
     const size_t n = (size_t)std::max<int32_t>(max_subvols, 1);
-    return v * sizeof(float) * 9 + n * sizeof(SubVolDev) + 3 * (n + 1) * sizeof(int) + 256;
+    return v * sizeof(float) * 9 + n * sizeof(SubVolDev) + rsf::NKERN * (n + 1) * sizeof(int) + 256;
 }
 
 static void ws_free(rsf_workspace *ws) {
@@ -172,10 +172,10 @@ rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_wor
     alloc((void **)&ws->pool_x, 4 * v * sizeof(float));
     alloc((void **)&ws->pool_y, 4 * v * sizeof(float));
     alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
-    alloc((void **)&ws->d_pre, 3 * ((size_t)max_subvols + 1) * sizeof(int));
+    alloc((void **)&ws->d_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
     alloc((void **)&ws->d_flag, 256);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, (size_t)max_subvols * sizeof(SubVolDev));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_pre, 3 * ((size_t)max_subvols + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws->table_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws->capture_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMemset(ws->d_flag, 0, 256);
@@ -226,8 +226,8 @@ rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
 }
 
 // Lays out a batch in the workspace pools and uploads the table.
-rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, rsf_dtype dtype,
-                   const float *const *phi_out_override, int totals[3], cudaStream_t st) {
+rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, rsf_dtype dtype,
+                   const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, cudaStream_t st) {
     if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
     if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
@@ -244,9 +244,16 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, r
         if (e != cudaSuccess) return cuda_fail(e, "table event");
         ws->table_pending = false;
     }
+    std::vector<int> wv(n);
+    for (int i = 0; i < n; i++) {
+        int Wv, Hv, Lv, Wp;
+        rsf::valid_extents((int)svs[i].W, (int)svs[i].H, (int)svs[i].L, k, Wv, Hv, Lv, Wp);
+        wv[i] = Wv;
+    }
+    *xb_w = rsf::choose_xb(wv.data(), n);
     const int n1 = n + 1;
     int *pre = ws->h_pre;
-    pre[0] = pre[n1] = pre[2 * n1] = 0;
+    for (int j = 0; j < rsf::NKERN; j++) pre[j * n1] = 0;
     size_t off_v = 0, off_x = 0, off_y = 0;
     for (int i = 0; i < n; i++) {
         SubVolDev d;
@@ -254,37 +261,43 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, r
         d.W = (int)svs[i].W;
         d.H = (int)svs[i].H;
         d.L = (int)svs[i].L;
-        rsf::tile_counts(d.W, d.H, d.L, k, d.tiles, d.Wv, d.Hv, d.Lv);
+        rsf::valid_extents(d.W, d.H, d.L, k, d.Wv, d.Hv, d.Lv, d.Wp);
+        int tiles[rsf::NKERN];
+        rsf::tile_counts(d, kspec, *xb_w, tiles);
         const size_t nv = (size_t)d.W * d.H * d.L;
         d.phi[0] = svs[i].phi;
         d.phi[1] = phi_out_override ? const_cast<float *>(phi_out_override[i]) : ws->pool_phi2 + off_v;
         d.img = svs[i].image;
         d.xb = ws->pool_x + off_x;
+        d.db = d.xb;  // the data factor reuses the x-pass storage
         d.yb = ws->pool_y + off_y;
         off_v += nv;
-        off_x += 4 * (size_t)d.Wv * d.H * d.L;
-        off_y += 4 * (size_t)d.Wv * d.Hv * d.L;
-        for (int j = 0; j < 3; j++) {
-            const int64_t next = (int64_t)pre[j * n1 + i] + d.tiles[j];
+        off_x += 4 * (size_t)d.Wp * d.H * d.L;
+        off_y += 4 * (size_t)d.Wp * d.Hv * d.L;
+        for (int j = 0; j < rsf::NKERN; j++) {
+            const int64_t next = (int64_t)pre[j * n1 + i] + tiles[j];
             if (next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");
             pre[j * n1 + i + 1] = (int)next;
         }
         ws->h_svs[i] = d;
     }
-    for (int j = 0; j < 3; j++) totals[j] = pre[j * n1 + n];
+    for (int j = 0; j < rsf::NKERN; j++) totals[j] = pre[j * n1 + n];
     cudaError_t e = cudaMemcpyAsync(ws->d_svs, ws->h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ws->d_pre, ws->h_pre, 3 * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(ws->d_pre, ws->h_pre, rsf::NKERN * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaEventRecord(ws->table_ev, st);
     if (e != cudaSuccess) return cuda_fail(e, "table upload");
     ws->table_pending = true;
     return RSF_OK;
 }
 
-StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n) {
+StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n, int xb_w) {
     StepConst c;
     std::memset(&c, 0, sizeof c);
-    for (int i = 0; i < k; i++) c.taps[i] = taps[i];
+    for (int i = 0; i < k; i++) {
+        c.taps[i] = taps[i];
+        c.taps2[i] = make_float2(taps[i], taps[i]);
+    }
     c.k = k;
     c.r = (k - 1) / 2;
     c.eps = p->eps;
@@ -297,6 +310,7 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.boundary = p->boundary;
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
+    c.xb_w = xb_w;
     return c;
 }
 
@@ -321,11 +335,11 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     int k = 0;
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
-    int tot[3];
-    s = prepare(ws, svs, n, k, dtype, nullptr, tot, st);
+    int tot[rsf::NKERN], xb_w = 0;
+    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false), dtype, nullptr, tot, &xb_w, st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
-    const StepConst c = make_const(p, k, taps, dtype, n);
+    const StepConst c = make_const(p, k, taps, dtype, n, xb_w);
     cudaError_t e = cudaSuccess;
     if (!use_graph) {
         for (int it = 0; it < iters && e == cudaSuccess; it++)
@@ -421,11 +435,11 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     if (s != RSF_OK) return s;
     rsf_subvol sv = {const_cast<float *>(phi), image, W, H, L};
     const float *outs[1] = {phi_out};
-    int tot[3];
+    int tot[rsf::NKERN], xb_w = 0;
     cudaStream_t st = (cudaStream_t)stream;
-    s = prepare(ws, &sv, 1, k, dtype, outs, tot, st);
+    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), dtype, outs, tot, &xb_w, st);
     if (s != RSF_OK) return s;
-    const StepConst c = make_const(p, k, taps, dtype, 1);
+    const StepConst c = make_const(p, k, taps, dtype, 1, xb_w);
     const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};
     cudaError_t e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, 0, p->arith, ws->d_flag, &dbg, st);
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");

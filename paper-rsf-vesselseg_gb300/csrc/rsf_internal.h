@@ -7,51 +7,88 @@ namespace rsf {
 
 constexpr int MAXK = 128;  // largest supported tap count (sigma up to ~18)
 
-// Tilings (fixed at compile time; the launchers derive tile counts from them).
-constexpr int XP_ROWS = 8;    // x-pass: rows per block (one warp per row)
-constexpr int XP_XB = 5;      // x-pass: outputs per lane (odd: conflict-free smem)
-constexpr int XP_TX = 32 * XP_XB;
-constexpr int YP_TX = 128;    // y-pass: threads along x
-constexpr int YP_YB = 16;     // y-pass: outputs per thread along y
-constexpr int UP_TX = 32;     // update: tile width (x)
-constexpr int UP_TY = 8;      // update: tile height (y)
-constexpr int UP_ZB = 16;     // update: planes per block (z)
+// Kernel tilings (the launchers derive tile counts from them).
+constexpr int XP_ROWS = 8;     // x-pass: rows per block (one warp per row)
+constexpr int YP_PAIRS = 128;  // y-pass: column pairs per block (one thread each)
+constexpr int YB_TX = 128;     // generic y-pass: columns per block
+constexpr int YB_YB = 16;      // generic y-pass: outputs per thread along y
+constexpr int ZP_PAIRS = 32;   // z-pass: column pairs per block (four lanes each)
+constexpr int ZB_TX = 128;     // generic z-pass: columns per block
+constexpr int ZB_ZB = 16;      // generic z-pass: outputs per thread along z
+constexpr int ST_OX = 30;      // stencil: output columns per warp (lanes 1..30)
+constexpr int ST_OY = 14;      // stencil: output rows per block (warps 1..14)
+constexpr int ST_WARPS = ST_OY + 2;
+constexpr int ST_ZC = 32;      // stencil: planes per block
+
+// The x-pass lane width (outputs per lane) is chosen per launch from these.
+constexpr int XB_CHOICES[2] = {5, 9};
 
 // One sub-volume as the kernels see it.
+//   xb: 4 x-pass fields, each Wp x H x L   (row stride Wp)
+//   yb: 4 y-pass fields, each Wp x Hv x L
+//   db: data factor lambda (e_out - e_in) of the valid region, Wp x Hv x Lv;
+//       it reuses the x-pass storage, which is dead once the y-pass has run.
 struct SubVolDev {
     float *phi[2];       // ping-pong level-set buffers
     const void *img;     // image, uint8 or float32
-    float *xb;           // 4 fields of the x-pass, each Wv*H*L
-    float *yb;           // 4 fields of the y-pass, each Wv*Hv*L
+    float *xb;
+    float *yb;
+    float *db;
     int W, H, L;
-    int Wv, Hv, Lv;      // valid extents of the blur (<= 0: all border)
-    int tiles[3];        // blocks of x-pass, y-pass, update
+    int Wv, Hv, Lv;      // valid extents of the blur (0: all border)
+    int Wp;              // padded row stride of xb / yb / db (multiple of 4)
     int pad;
 };
 
 // Per-launch constants, passed by value (they live in the constant bank).
 struct StepConst {
     float taps[MAXK];
+    float2 taps2[MAXK];  // (g, g) pairs for the packed multiply-adds
     int k, r;
     float eps, dt, mu, nu, l1, l2;
     int lam_equal;
     int boundary;   // 0 reference (x = 0 wraps to the previous row), 1 clamp
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
+    int xb_w;       // x-pass outputs per lane for this launch
 };
 
-// Optional per-voxel debug outputs of the update kernel (8 fields).
+// Optional per-voxel debug outputs (8 fields, full-volume layout).
 struct DebugOut {
-    float *f;       // 8 * N floats, field-major
+    float *f;
     int64_t n;
 };
 
-cudaError_t launch_step(const SubVolDev *d_svs, const int *d_pre, const int *h_pre_tot,
-                        const StepConst &c, int parity, int arith, unsigned *d_flag,
-                        const DebugOut *dbg, cudaStream_t st);
+constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil
+
+// Tap counts with streaming (compile-time K) kernels.  Other tap counts, the
+// debug step and the reference arithmetic use the run-time-k kernels.
+inline bool is_specialised(int k) { return k == 21 || k == 29 || k == 35; }
+inline int kernel_k(int k, int arith, bool debug) { return (is_specialised(k) && arith == 0 && !debug) ? k : 0; }
+
+// Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
+void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]);
+int choose_xb(const int *Wv, int n);
+void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
+
+cudaError_t launch_step(const SubVolDev *d_svs, const int *d_pre, const int *h_tot, const StepConst &c,
+                        int parity, int arith, unsigned *d_flag, const DebugOut *dbg, cudaStream_t st);
 
 cudaError_t configure_device();
 
-void tile_counts(int W, int H, int L, int k, int tiles[3], int &Wv, int &Hv, int &Lv);
+// Per-kernel launchers; each tap specialisation lives in its own object file.
+#define RSF_DECLARE_K(K)                                                                                      \
+    cudaError_t launch_xpass_##K(const SubVolDev *, const int *, int, const StepConst &, int, int, cudaStream_t); \
+    cudaError_t config_xpass_##K();                                                                             \
+    cudaError_t launch_ypass_##K(const SubVolDev *, const int *, int, const StepConst &, cudaStream_t);          \
+    cudaError_t launch_zpass_##K(const SubVolDev *, const int *, int, const StepConst &, const DebugOut *,      \
+                                 cudaStream_t);
+RSF_DECLARE_K(0)
+RSF_DECLARE_K(21)
+RSF_DECLARE_K(29)
+RSF_DECLARE_K(35)
+#undef RSF_DECLARE_K
+cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
+                           unsigned *flag, const DebugOut *dbg, cudaStream_t);
 
 }  // namespace rsf

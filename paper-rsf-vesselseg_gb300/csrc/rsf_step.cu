@@ -1,0 +1,92 @@
+// rsf_step.cu -- host side of one RSF iteration: tilings and the launch
+// sequence x-pass -> y-pass -> z-pass -> stencil.
+#include <cuda_runtime.h>
+
+#include "rsf_internal.h"
+
+namespace rsf {
+
+void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp) {
+    Wv = W - k + 1;
+    Hv = H - k + 1;
+    Lv = L - k + 1;
+    if (Wv <= 0 || Hv <= 0 || Lv <= 0) Wv = Hv = Lv = 0;
+    Wp = (Wv + 3) & ~3;
+}
+
+// Lane width of the x-pass that computes the fewest wasted outputs.
+int choose_xb(const int *Wv, int n) {
+    int best = XB_CHOICES[0];
+    long long best_cost = -1;
+    for (int xb : XB_CHOICES) {
+        const long long xt = 32LL * xb;
+        long long cost = 0;
+        for (int i = 0; i < n; i++) cost += ((Wv[i] + xt - 1) / xt) * xt;
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = xb;
+        }
+    }
+    return best;
+}
+
+void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]) {
+    const bool valid = d.Wv > 0;
+    const int xt = 32 * xb_w;
+    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L : 0;
+    if (!valid) tiles[1] = 0;
+    else if (kspec == 0) tiles[1] = ((d.Wv + YB_TX - 1) / YB_TX) * ((d.Hv + YB_YB - 1) / YB_YB) * 4 * d.L;
+    else tiles[1] = ((d.Wv + 2 * YP_PAIRS - 1) / (2 * YP_PAIRS)) * 4 * d.L;
+    if (!valid) tiles[2] = 0;
+    else if (kspec == 0) tiles[2] = ((d.Wv + ZB_TX - 1) / ZB_TX) * ((d.Lv + ZB_ZB - 1) / ZB_ZB) * d.Hv;
+    else tiles[2] = ((d.Wv + 2 * ZP_PAIRS - 1) / (2 * ZP_PAIRS)) * d.Hv;
+    tiles[3] = ((d.W + ST_OX - 1) / ST_OX) * ((d.H + ST_OY - 1) / ST_OY) * ((d.L + ST_ZC - 1) / ST_ZC);
+}
+
+// Raises the dynamic shared-memory limit of the x-pass instantiations on the
+// current device; called once per workspace, outside any stream capture.
+cudaError_t configure_device() {
+    cudaError_t e = config_xpass_0();
+    if (e == cudaSuccess) e = config_xpass_21();
+    if (e == cudaSuccess) e = config_xpass_29();
+    if (e == cudaSuccess) e = config_xpass_35();
+    return e;
+}
+
+cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, const StepConst &c, int parity,
+                        int arith, unsigned *flag, const DebugOut *dbg, cudaStream_t st) {
+    const int n1 = c.nsv + 1;
+    const int kspec = kernel_k(c.k, arith, dbg != nullptr);
+    cudaError_t e = cudaSuccess;
+    if (tot[0] > 0) {
+        switch (kspec) {
+            case 21: e = launch_xpass_21(svs, pre, tot[0], c, parity, arith, st); break;
+            case 29: e = launch_xpass_29(svs, pre, tot[0], c, parity, arith, st); break;
+            case 35: e = launch_xpass_35(svs, pre, tot[0], c, parity, arith, st); break;
+            default: e = launch_xpass_0(svs, pre, tot[0], c, parity, arith, st); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    if (tot[1] > 0) {
+        switch (kspec) {
+            case 21: e = launch_ypass_21(svs, pre + n1, tot[1], c, st); break;
+            case 29: e = launch_ypass_29(svs, pre + n1, tot[1], c, st); break;
+            case 35: e = launch_ypass_35(svs, pre + n1, tot[1], c, st); break;
+            default: e = launch_ypass_0(svs, pre + n1, tot[1], c, st); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    if (tot[2] > 0) {
+        switch (kspec) {
+            case 21: e = launch_zpass_21(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
+            case 29: e = launch_zpass_29(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
+            case 35: e = launch_zpass_35(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
+            default: e = launch_zpass_0(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    if (tot[3] > 0) e = launch_stencil(svs, pre + 3 * n1, tot[3], c, parity, arith, flag, dbg, st);
+    return e;
+}
+
+}  // namespace rsf

@@ -1,0 +1,27 @@
+// rsf_zpass.cu -- z-pass (local fits and data factor) for one tap count
+// (compiled once per -DRSF_K value; RSF_K = 0 is the run-time-k kernel, which
+// also writes the debug fields).
+#include "rsf_kernels.cuh"
+
+#ifndef RSF_K
+#error "compile with -DRSF_K=<taps>"
+#endif
+#define RSF_CAT2(a, b) a##b
+#define RSF_CAT(a, b) RSF_CAT2(a, b)
+
+namespace rsf {
+
+cudaError_t RSF_CAT(launch_zpass_, RSF_K)(const SubVolDev *svs, const int *pre, int blocks, const StepConst &c,
+                                          const DebugOut *dbg, cudaStream_t st) {
+    const DebugOut none = {nullptr, 0};
+#if RSF_K > 0
+    (void)dbg;
+    zpass_kernel<RSF_K, false><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
+#else
+    if (dbg) zpass_generic_kernel<true><<<blocks, ZB_TX, 0, st>>>(svs, pre, c, *dbg);
+    else zpass_generic_kernel<false><<<blocks, ZB_TX, 0, st>>>(svs, pre, c, none);
+#endif
+    return cudaGetLastError();
+}
+
+}  // namespace rsf

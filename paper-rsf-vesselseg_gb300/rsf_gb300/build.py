@@ -24,7 +24,12 @@ CLI_PATH = BIN_DIR / "rsf3d"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
                      "-I", str(INCLUDE), "-I", str(CSRC)]
-CU_SOURCES = ["rsf_forward.cu", "rsf_capi.cu"]
+# (source, object stem, extra defines): the per-family kernels are compiled
+# once per tap specialisation so that the objects build in parallel.
+CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in ("xpass", "ypass", "zpass")
+             for k in (0, 21, 29, 35)]
+            + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
+               ("rsf_capi.cu", "rsf_capi", [])])
 CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp", "sdf.cpp"]
 
 
@@ -59,11 +64,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     nv = nvcc()
     jobs = []
     objs = []
-    for src in CU_SOURCES:
-        obj = BUILD_DIR / (Path(src).stem + ".o")
+    for src, stem, defs in CU_UNITS:
+        obj = BUILD_DIR / (stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
-            flags = NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else [])
+            flags = NVCC_FLAGS + defs + (["-Xptxas", "-v"] if ptxas_info else [])
             jobs.append([nv, *flags, "-c", CSRC / src, "-o", obj])
     cli_objs = []
     for src in CLI_SOURCES:
