@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of batched RSF level-set evolution on GB300.
+
+Workload: 48 overlapping sub-volumes of uneven shape (extents 64-320 voxels)
+cut from a 512 x 1024 x 1024 synthetic vessel volume (800 Catmull-Rom tubes,
+radius U[1.5, 8], vessel N(180,20), background N(40,15), noise N(0,10), sine
+bias field), phi0 the +-3-clipped signed distance of a per-tube dilated or
+eroded mask; sigma 3 (21 taps), lambda1 = lambda2 = 1, mu 1,
+nu 0.001*255^2, eps 1, dt 0.1, 150 iterations.  One step = one full
+150-iteration evolution of all 48 sub-volumes (one batched call, the
+iteration loop replayed from a captured CUDA graph).
+
+Metric: Gvoxel-iterations/s (voxels of all sub-volumes, halos included,
+times iterations, per second), aggregated over ranks.  With --gpus N every
+rank evolves its own 48-sub-volume batch (weak scaling, no collective on
+the data path).
+
+--impl reference times the CPU oracle (the restatement of the reference's
+kernel.cu arithmetic; the reference has no CPU implementation of its own)
+on the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "paper-rsf-vesselseg_gb300"))
+
+METRIC = "Gvoxel-iterations/s (batched RSF evolution)"
+UNIT = "Gvoxel-iter/s"
+ITERS = 150
+SIGMA = 3.0
+PARAMS = dict(sigma=SIGMA, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=0.001 * 255.0 ** 2, eps=1.0)
+WORKLOAD = ("config2: 48 uneven sub-volumes (extents 64-320 per axis, 256^3 cores + 32-voxel halos) cut from a "
+            "512x1024x1024 synthetic vessel volume (800 tubes, radius U[1.5,8]); sigma 3 (21 taps), lambda 1, mu 1, "
+            "nu 0.001*255^2, eps 1, dt 0.1; 150 iterations; phi float32, image uint8")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def algorithmic_bytes(tiles, k):
+    """Bytes each kernel must move once per launch over the whole batch:
+    x-pass reads phi (4) and I (1) and writes 4 fields of the x-valid extent;
+    y-pass reads those and writes 4 fields of the xy-valid extent; z-pass
+    reads those and I and writes the data factor of the valid region; the
+    stencil reads phi and the data factor and writes phi."""
+    out = {"xpass": 0, "ypass": 0, "zpass": 0, "stencil": 0}
+    for t in tiles:
+        L, H, W = t.shape
+        Wv, Hv, Lv = max(W - k + 1, 0), max(H - k + 1, 0), max(L - k + 1, 0)
+        if min(Wv, Hv, Lv) == 0:
+            Wv = Hv = Lv = 0
+        n = W * H * L
+        out["xpass"] += 5 * n + 16 * Wv * H * L
+        out["ypass"] += 16 * Wv * H * L + 16 * Wv * Hv * L
+        out["zpass"] += 16 * Wv * Hv * L + 5 * Wv * Hv * Lv
+        out["stencil"] += 12 * n
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per voxel of `kernel` from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic_per_voxel.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get("kernels", {}).get(kernel)
+
+
+def cpu_sample(threads: int, budget_s: float = 15.0):
+    """Times the CPU oracle on one sub-volume of the workload's shape class
+    (the 64 x 288 x 288 corner tile), iterations sized to ~budget_s."""
+    import numpy as np
+
+    from oracle import rsf_oracle as orc
+    from rsf_gb300 import synth
+
+    shape = (64, 288, 288)
+    img, phi0, _ = synth.make_volume(synth.VolumeSpec(shape, 12, 1.5, 8.0, 20))
+    p = orc.params(**{k: v for k, v in PARAMS.items()})
+    imgf = img.astype(np.float32)
+    t0 = time.perf_counter()
+    orc.evolve(phi0, imgf, p, 1, threads)
+    one = max(time.perf_counter() - t0, 1e-3)
+    iters = int(max(2, min(200, budget_s / one)))
+    t0 = time.perf_counter()
+    orc.evolve(phi0, imgf, p, iters, threads)
+    dt = time.perf_counter() - t0
+    vox = img.size * iters
+    return {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"CPU oracle (C, OpenMP, {threads} threads), one {shape[2]}x{shape[1]}x{shape[0]} sub-volume "
+                      f"of the workload's shape class, {iters} iterations, {dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    from oracle import rsf_oracle as orc
+    from rsf_gb300 import synth
+
+    threads = os.cpu_count() or 1
+    shape = (64, 288, 288)
+    img, phi0, _ = synth.make_volume(synth.VolumeSpec(shape, 12, 1.5, 8.0, 20))
+    imgf = img.astype(np.float32)
+    p = orc.params(**PARAMS)
+    iters_per_step = 10
+    for _ in range(args.warmup):
+        orc.evolve(phi0, imgf, p, iters_per_step, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.evolve(phi0, imgf, p, iters_per_step, threads)
+    dt = time.perf_counter() - t0
+    value = img.size * iters_per_step * args.steps / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "reference_step": f"{iters_per_step} iterations of one {shape[2]}x{shape[1]}x"
+                   f"{shape[0]} sub-volume of the workload (bounded CPU sample)", "parallelism": f"dp{args.gpus}"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"CPU oracle (C, OpenMP, {threads} threads); the reference has no CPU code path"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from rsf_gb300 import Params, Workspace, synth, tiling
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    # ---- inputs resident in HBM --------------------------------------
+    spec = synth.VolumeSpec(synth.CONFIG2.shape, synth.CONFIG2.n_tubes, synth.CONFIG2.r_min, synth.CONFIG2.r_max,
+                            synth.CONFIG2.seed + rank)
+    img_full, phi_full, _ = synth.make_volume_torch(spec, dev)
+    tiles = tiling.config2_tiles()
+    imgs = [img_full[t.slices()].contiguous() for t in tiles]
+    phi0s = [phi_full[t.slices()].contiguous() for t in tiles]
+    del img_full, phi_full
+    torch.cuda.empty_cache()
+    work = [p.clone() for p in phi0s]
+    total_vox = sum(t.voxels for t in tiles)
+    p = Params(**PARAMS)
+    from rsf_gb300 import gaussian_taps
+
+    k = len(gaussian_taps(SIGMA))
+    ws = Workspace(total_vox, len(tiles))
+    pairs = list(zip(imgs, work))
+
+    def step():
+        for w, p0 in zip(work, phi0s):
+            w.copy_(p0)
+        ws.evolve_batched(pairs, p, ITERS)
+
+    for _ in range(args.warmup):
+        step()
+    ws.check()
+    torch.cuda.synchronize()
+
+    # ---- timed region ------------------------------------------------
+    ws.set_kernel_timing(True)
+    ws.kernel_times(reset=True)
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    kt = ws.kernel_times(reset=True)
+    ws.set_kernel_timing(False)
+    ws.check()
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    vox_iters = total_vox * ITERS * args.steps * world
+    value = vox_iters / (ms / 1e3) / 1e9
+
+    # ---- plain per-volume path (one sub-volume at a time, no graph) ----
+    for w, p0 in zip(work, phi0s):
+        w.copy_(p0)
+    torch.cuda.synchronize()
+    e0.record()
+    for (im, w) in pairs:
+        ws.evolve(im, w, p, ITERS)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_value = total_vox * ITERS / (plain_ms / 1e3) / 1e9
+
+    # ---- end to end: pinned host buffers -> evolve -> host ------------
+    h_imgs = [im.cpu().pin_memory() for im in imgs]
+    h_phis = [p0.cpu().pin_memory() for p0 in phi0s]
+    h_out = [torch.empty_like(hp).pin_memory() for hp in h_phis]
+    d_imgs = [torch.empty_like(im) for im in imgs]
+    h2d = sum(x.numel() * x.element_size() for x in h_imgs) + sum(x.numel() * 4 for x in h_phis)
+    d2h = sum(x.numel() * 4 for x in h_phis)
+
+    def e2e_step():
+        for d, h in zip(d_imgs, h_imgs):
+            d.copy_(h, non_blocking=True)
+        for w, h in zip(work, h_phis):
+            w.copy_(h, non_blocking=True)
+        ws.evolve_batched(list(zip(d_imgs, work)), p, ITERS)
+        for o, w in zip(h_out, work):
+            o.copy_(w, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = total_vox * ITERS * world / e2e_s / 1e9
+
+    # ---- roofline of the dominant kernel ------------------------------
+    alg = algorithmic_bytes(tiles, k)
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    for name, (kms, nl) in kt.items():
+        if nl == 0:
+            continue
+        per = kms / nl
+        kernels[name] = {"launches": int(nl), "ms_per_launch": per, "share": kms / max(1e-9, sum(v[0] for v in kt.values())),
+                         "alg_bytes_per_launch": alg[name], "gbs": alg[name] / (per / 1e3) / 1e9}
+    dom = max(kernels, key=lambda n: kernels[n]["ms_per_launch"] * kernels[n]["launches"])
+    dk = kernels[dom]
+    tr = ncu_traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": dk["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": dk["gbs"] / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": (tr * total_vox if tr is not None else None),
+                "step_alg_bytes_per_voxel_iter": sum(alg.values()) / total_vox,
+                "step_gbs": sum(alg.values()) * ITERS * args.steps / (ms / 1e3) / 1e9}
+    launches = sum(v[1] for v in kt.values())
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "subvolumes": len(tiles), "voxels": total_vox, "iterations": ITERS,
+                       "sigma": SIGMA, "taps": k, "step": "one 150-iteration evolution of all 48 sub-volumes",
+                       "l2": "inputs larger than L2 (phi 3.8 GB, y-pass fields 14 GB per iteration)",
+                       "parallelism": f"dp{world}"},
+            "plain": {"value": plain_value, "unit": UNIT,
+                      "how": "same sub-volumes evolved one at a time (rsf_evolve, no graph)"},
+            "batched_vs_plain": value / world / plain_value,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "kernels": kernels,
+            "clocks": clk,
+        }
+        if world == 1:
+            line["cpu_baseline"] = cpu_sample(os.cpu_count() or 1)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

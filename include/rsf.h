@@ -146,6 +146,13 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
                           rsf_dtype dtype, const float *phi, float *phi_out, float *fields,
                           int64_t W, int64_t H, int64_t L, void *stream);
 
+/* Per-kernel device timing.  When enabled, every evolution records CUDA
+ * events before and after each of its four kernels (x-pass, y-pass, z-pass,
+ * stencil/update), inside captured graphs too; rsf_kernel_times waits for
+ * them and returns the accumulated milliseconds and launch counts. */
+rsf_status rsf_set_kernel_timing(rsf_workspace *ws, int enable);
+rsf_status rsf_kernel_times(rsf_workspace *ws, double ms[4], int64_t launches[4], int reset);
+
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);

@@ -57,6 +57,13 @@ struct rsf_workspace {
     void *stage_img = nullptr;
     float *stage_phi = nullptr;
     size_t stage_voxels = 0;
+    // per-kernel timing (rsf_set_kernel_timing): events between launches
+    bool timing = false;
+    std::vector<cudaEvent_t> events;
+    int pending_iters = 0;            // iterations whose events are not read yet
+    int pending_tot[rsf::NKERN] = {0, 0, 0, 0};
+    double kernel_ms[rsf::NKERN] = {0, 0, 0, 0};
+    long long kernel_launches[rsf::NKERN] = {0, 0, 0, 0};
 };
 
 extern "C" {
@@ -145,6 +152,7 @@ static void ws_free(rsf_workspace *ws) {
     cudaFreeHost(ws->h_svs);
     cudaFreeHost(ws->h_pre);
     if (ws->table_ev) cudaEventDestroy(ws->table_ev);
+    for (cudaEvent_t ev : ws->events) cudaEventDestroy(ev);
     if (ws->capture_stream) cudaStreamDestroy(ws->capture_stream);
     if (cur >= 0) cudaSetDevice(cur);
     delete ws;
@@ -327,6 +335,41 @@ rsf_status copy_back(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, cudaSt
     return RSF_OK;
 }
 
+// Reads the events of the last timed evolution into the per-kernel totals.
+rsf_status collect_times(rsf_workspace *ws) {
+    if (ws->pending_iters == 0) return RSF_OK;
+    cudaError_t e = cudaEventSynchronize(ws->events[(size_t)rsf::NKERN * ws->pending_iters]);
+    if (e != cudaSuccess) return cuda_fail(e, "timing events");
+    for (int it = 0; it < ws->pending_iters; it++)
+        for (int j = 0; j < rsf::NKERN; j++) {
+            float ms = 0.0f;
+            e = cudaEventElapsedTime(&ms, ws->events[(size_t)rsf::NKERN * it + j],
+                                     ws->events[(size_t)rsf::NKERN * it + j + 1]);
+            if (e != cudaSuccess) return cuda_fail(e, "timing events");
+            ws->kernel_ms[j] += ms;
+            if (ws->pending_tot[j] > 0) ws->kernel_launches[j]++;
+        }
+    ws->pending_iters = 0;
+    return RSF_OK;
+}
+
+// Events for `iters` timed iterations: NKERN per iteration plus one, each
+// iteration's last event being the next one's first.
+rsf_status timing_events(rsf_workspace *ws, int iters, const int tot[rsf::NKERN]) {
+    rsf_status s = collect_times(ws);
+    if (s != RSF_OK) return s;
+    const size_t need = (size_t)rsf::NKERN * iters + 1;
+    while (ws->events.size() < need) {
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) return cuda_fail(e, "event create");
+        ws->events.push_back(ev);
+    }
+    ws->pending_iters = iters;
+    for (int j = 0; j < rsf::NKERN; j++) ws->pending_tot[j] = tot[j];
+    return RSF_OK;
+}
+
 rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rsf_subvol *svs, int32_t n,
                int32_t iters, cudaStream_t st, bool use_graph) {
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
@@ -340,33 +383,47 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
     const StepConst c = make_const(p, k, taps, dtype, n, xb_w);
+    if (ws->timing) {
+        s = timing_events(ws, iters, tot);
+        if (s != RSF_OK) return s;
+    }
+    auto step = [&](int it, cudaStream_t on) {
+        cudaEvent_t *ev = ws->timing ? &ws->events[(size_t)rsf::NKERN * it] : nullptr;
+        return rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, it & 1, p->arith, ws->d_flag, nullptr, on, ev);
+    };
     cudaError_t e = cudaSuccess;
     if (!use_graph) {
-        for (int it = 0; it < iters && e == cudaSuccess; it++)
-            e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, it & 1, p->arith, ws->d_flag, nullptr, st);
+        for (int it = 0; it < iters && e == cudaSuccess; it++) e = step(it, st);
         if (e != cudaSuccess) return cuda_fail(e, "step launch");
     } else {
-        // Capture two iterations (phi -> phi2 -> phi) once, replay them.
-        auto capture = [&](int count, cudaGraphExec_t *exec) -> cudaError_t {
+        // Capture iterations [first, first + count) into one executable graph.
+        auto capture = [&](int first, int count, cudaGraphExec_t *exec) -> cudaError_t {
             cudaGraph_t g = nullptr;
             cudaError_t err = cudaStreamBeginCapture(ws->capture_stream, cudaStreamCaptureModeThreadLocal);
             if (err != cudaSuccess) return err;
-            for (int it = 0; it < count && err == cudaSuccess; it++)
-                err = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, it & 1, p->arith, ws->d_flag, nullptr,
-                                       ws->capture_stream);
+            for (int it = first; it < first + count && err == cudaSuccess; it++) err = step(it, ws->capture_stream);
             cudaError_t end = cudaStreamEndCapture(ws->capture_stream, &g);
             if (err == cudaSuccess) err = end;
             if (err == cudaSuccess) err = cudaGraphInstantiate(exec, g, 0);
             if (g) cudaGraphDestroy(g);
             return err;
         };
-        cudaGraphExec_t pair = nullptr, single = nullptr;
-        if (iters >= 2) e = capture(2, &pair);
-        if (e == cudaSuccess && (iters & 1)) e = capture(1, &single);
-        for (int i = 0; i < iters / 2 && e == cudaSuccess; i++) e = cudaGraphLaunch(pair, st);
-        if (e == cudaSuccess && single) e = cudaGraphLaunch(single, st);
-        if (pair) cudaGraphExecDestroy(pair);
-        if (single) cudaGraphExecDestroy(single);
+        if (ws->timing) {
+            // every iteration has its own events: capture the whole evolution
+            cudaGraphExec_t all = nullptr;
+            e = capture(0, iters, &all);
+            if (e == cudaSuccess) e = cudaGraphLaunch(all, st);
+            if (all) cudaGraphExecDestroy(all);
+        } else {
+            // two iterations (phi -> phi2 -> phi) captured once and replayed
+            cudaGraphExec_t pair = nullptr, single = nullptr;
+            if (iters >= 2) e = capture(0, 2, &pair);
+            if (e == cudaSuccess && (iters & 1)) e = capture(0, 1, &single);
+            for (int i = 0; i < iters / 2 && e == cudaSuccess; i++) e = cudaGraphLaunch(pair, st);
+            if (e == cudaSuccess && single) e = cudaGraphLaunch(single, st);
+            if (pair) cudaGraphExecDestroy(pair);
+            if (single) cudaGraphExecDestroy(single);
+        }
         if (e != cudaSuccess) return cuda_fail(e, "graph");
     }
     if (iters & 1) return copy_back(ws, svs, n, st);
@@ -456,6 +513,29 @@ rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
     if (e == cudaSuccess && flag) e = cudaMemset(ws->d_flag, 0, sizeof flag);
     if (e != cudaSuccess) return cuda_fail(e, "flag read");
     if (flag) return fail(RSF_ERR_NONFINITE, "non-finite value written to phi");
+    return RSF_OK;
+}
+
+rsf_status rsf_set_kernel_timing(rsf_workspace *ws, int enable) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    rsf_status s = collect_times(ws);
+    if (s != RSF_OK) return s;
+    ws->timing = enable != 0;
+    return RSF_OK;
+}
+
+rsf_status rsf_kernel_times(rsf_workspace *ws, double ms[4], int64_t launches[4], int reset) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    rsf_status s = collect_times(ws);
+    if (s != RSF_OK) return s;
+    for (int j = 0; j < rsf::NKERN; j++) {
+        if (ms) ms[j] = ws->kernel_ms[j];
+        if (launches) launches[j] = ws->kernel_launches[j];
+        if (reset) {
+            ws->kernel_ms[j] = 0.0;
+            ws->kernel_launches[j] = 0;
+        }
+    }
     return RSF_OK;
 }
 

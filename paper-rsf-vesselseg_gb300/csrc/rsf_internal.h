@@ -71,8 +71,11 @@ void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]);
 int choose_xb(const int *Wv, int n);
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
 
+// One iteration.  With `ev` (NKERN + 1 events) the events are recorded before
+// the first and after every kernel, for per-kernel device times.
 cudaError_t launch_step(const SubVolDev *d_svs, const int *d_pre, const int *h_tot, const StepConst &c,
-                        int parity, int arith, unsigned *d_flag, const DebugOut *dbg, cudaStream_t st);
+                        int parity, int arith, unsigned *d_flag, const DebugOut *dbg, cudaStream_t st,
+                        cudaEvent_t *ev = nullptr);
 
 cudaError_t configure_device();
 

@@ -54,10 +54,14 @@ cudaError_t configure_device() {
 }
 
 cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, const StepConst &c, int parity,
-                        int arith, unsigned *flag, const DebugOut *dbg, cudaStream_t st) {
+                        int arith, unsigned *flag, const DebugOut *dbg, cudaStream_t st, cudaEvent_t *ev) {
     const int n1 = c.nsv + 1;
     const int kspec = kernel_k(c.k, arith, dbg != nullptr);
     cudaError_t e = cudaSuccess;
+    // External records so that, inside a stream capture, they become event
+    // record nodes of the graph (a plain record there only orders streams).
+    auto mark = [&](int i) { return ev ? cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal) : cudaSuccess; };
+    if ((e = mark(0)) != cudaSuccess) return e;
     if (tot[0] > 0) {
         switch (kspec) {
             case 21: e = launch_xpass_21(svs, pre, tot[0], c, parity, arith, st); break;
@@ -67,6 +71,7 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
         }
         if (e != cudaSuccess) return e;
     }
+    if ((e = mark(1)) != cudaSuccess) return e;
     if (tot[1] > 0) {
         switch (kspec) {
             case 21: e = launch_ypass_21(svs, pre + n1, tot[1], c, st); break;
@@ -76,6 +81,7 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
         }
         if (e != cudaSuccess) return e;
     }
+    if ((e = mark(2)) != cudaSuccess) return e;
     if (tot[2] > 0) {
         switch (kspec) {
             case 21: e = launch_zpass_21(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
@@ -85,7 +91,9 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
         }
         if (e != cudaSuccess) return e;
     }
+    if ((e = mark(3)) != cudaSuccess) return e;
     if (tot[3] > 0) e = launch_stencil(svs, pre + 3 * n1, tot[3], c, parity, arith, flag, dbg, st);
+    if (e == cudaSuccess) e = mark(4);
     return e;
 }
 

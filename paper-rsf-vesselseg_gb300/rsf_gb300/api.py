@@ -102,6 +102,18 @@ class Workspace:
     def __exit__(self, *exc):
         self.close()
 
+    def set_kernel_timing(self, enable: bool):
+        check(self._lib.rsf_set_kernel_timing(self.handle, int(bool(enable))))
+
+    KERNELS = ("xpass", "ypass", "zpass", "stencil")
+
+    def kernel_times(self, reset: bool = False):
+        """{kernel: (total ms, launches)} accumulated while timing was enabled."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_int64 * 4)()
+        check(self._lib.rsf_kernel_times(self.handle, ms, n, int(bool(reset))))
+        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS)}
+
     def check(self, stream=None):
         check(self._lib.rsf_workspace_check(self.handle, ctypes.c_void_p(_stream_ptr(stream))))
 

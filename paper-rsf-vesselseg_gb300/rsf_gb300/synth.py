@@ -164,3 +164,109 @@ def make_volume(spec: VolumeSpec):
 def make_small(shape=(24, 20, 18), n_tubes=3, r_min=1.5, r_max=3.0, seed=0):
     """A small instance of the same generator for unit tests."""
     return make_volume(VolumeSpec(tuple(shape), n_tubes, r_min, r_max, seed))
+
+
+# ---------------------------------------------------------------------------
+# Device path for gigavoxel volumes.  Same spec; tube geometry comes from the
+# same NumPy RNG stream, intensities from a seeded torch generator on the
+# device, and the perturbation is one dilation or erosion (radius 1-2) per
+# tube rather than per connected region.  The signed distance is exact up to
+# the clip: every voxel within `clip` of the opposite label is found by
+# checking all integer offsets of length <= clip.
+# ---------------------------------------------------------------------------
+CONFIG2 = VolumeSpec((512, 1024, 1024), 800, 1.5, 8.0, 2)
+CONFIG3 = VolumeSpec((1024, 1024, 1024), 2000, 1.0, 10.0, 3)
+
+
+def _stamp_tube_torch(mask_flat, shape, samples, radius):
+    import torch
+
+    Z, Y, X = shape
+    dev = mask_flat.device
+    rc = int(math.ceil(radius)) + 1
+    ax = torch.arange(-rc, rc + 1, device=dev)
+    oz, oy, ox = torch.meshgrid(ax, ax, ax, indexing="ij")
+    offs = torch.stack([ox.reshape(-1), oy.reshape(-1), oz.reshape(-1)], dim=1)
+    pts_all = torch.as_tensor(samples, dtype=torch.float32, device=dev)
+    r2 = float(radius) * float(radius)
+    chunk = max(1, 8_000_000 // offs.shape[0])
+    for s in range(0, pts_all.shape[0], chunk):
+        pts = pts_all[s:s + chunk]
+        vox = torch.floor(pts).long()[:, None, :] + offs[None, :, :]
+        d = vox.float() - pts[:, None, :]
+        hit = (d * d).sum(-1) <= r2
+        hit &= (vox[..., 0] >= 0) & (vox[..., 0] < X) & (vox[..., 1] >= 0) & (vox[..., 1] < Y)
+        hit &= (vox[..., 2] >= 0) & (vox[..., 2] < Z)
+        v = vox[hit]
+        mask_flat[(v[:, 2] * Y + v[:, 1]) * X + v[:, 0]] = True
+
+
+def signed_distance_torch(mask, clip: float = 3.0):
+    """Exact Euclidean signed distance (positive inside) clipped to +-clip."""
+    import torch
+
+    c = int(math.floor(clip))
+    Z, Y, X = mask.shape
+    pad = torch.full((Z + 2 * c, Y + 2 * c, X + 2 * c), 2, dtype=torch.int8, device=mask.device)
+    pad[c:c + Z, c:c + Y, c:c + X] = mask.to(torch.int8)
+    big = float(clip * clip)
+    d_in = torch.full(mask.shape, big, dtype=torch.float32, device=mask.device)
+    d_out = torch.full(mask.shape, big, dtype=torch.float32, device=mask.device)
+    inside = mask
+    outside = ~mask
+    for dz in range(-c, c + 1):
+        for dy in range(-c, c + 1):
+            for dx in range(-c, c + 1):
+                r2 = dz * dz + dy * dy + dx * dx
+                if r2 == 0 or r2 > clip * clip:
+                    continue
+                nb = pad[c + dz:c + dz + Z, c + dy:c + dy + Y, c + dx:c + dx + X]
+                d_in = torch.where(inside & (nb == 0), torch.clamp(d_in, max=float(r2)), d_in)
+                d_out = torch.where(outside & (nb == 1), torch.clamp(d_out, max=float(r2)), d_out)
+    return torch.where(inside, torch.sqrt(d_in), -torch.sqrt(d_out))
+
+
+def make_volume_torch(spec: VolumeSpec, device):
+    """Returns (I uint8, phi0 float32, true mask bool) as CUDA tensors."""
+    import torch
+
+    rng = np.random.default_rng(spec.seed)
+    Z, Y, X = spec.shape
+    hi = np.array([X - 1, Y - 1, Z - 1], dtype=np.float64)
+    true_flat = torch.zeros(Z * Y * X, dtype=torch.bool, device=device)
+    pert_flat = torch.zeros(Z * Y * X, dtype=torch.bool, device=device)
+    for _ in range(spec.n_tubes):
+        n_ctrl = int(rng.integers(4, 7))
+        ctrl = rng.uniform(0.0, 1.0, size=(n_ctrl, 3)) * hi
+        radius = float(rng.uniform(spec.r_min, spec.r_max))
+        delta = float(rng.choice([-2.0, -1.0, 1.0, 2.0]))
+        samples = _catmull_rom(ctrl)
+        _stamp_tube_torch(true_flat, spec.shape, samples, radius)
+        if radius + delta >= 0.5:
+            _stamp_tube_torch(pert_flat, spec.shape, samples, radius + delta)
+    mask = true_flat.view(Z, Y, X)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(spec.seed)
+    img = torch.empty((Z, Y, X), dtype=torch.float32, device=device)
+    for z0 in range(0, Z, 64):  # slabs bound the temporaries
+        sl = slice(z0, min(Z, z0 + 64))
+        m = mask[sl]
+        v = torch.randn(m.shape, generator=gen, device=device) * 20.0 + 180.0
+        b = torch.randn(m.shape, generator=gen, device=device) * 15.0 + 40.0
+        img[sl] = torch.where(m, v, b)
+    ph = rng.uniform(0.0, 1.0, size=3)
+    tz = torch.arange(Z, device=device, dtype=torch.float32)
+    ty = torch.arange(Y, device=device, dtype=torch.float32)
+    tx = torch.arange(X, device=device, dtype=torch.float32)
+    bz = torch.sin(2 * math.pi * (tz / Z + float(ph[2])))[:, None, None]
+    by = torch.sin(2 * math.pi * (ty / Y + float(ph[1])))[None, :, None]
+    bx = torch.sin(2 * math.pi * (tx / X + float(ph[0])))[None, None, :]
+    for z0 in range(0, Z, 64):
+        sl = slice(z0, min(Z, z0 + 64))
+        t = img[sl] * (1.0 + 0.3 * bz[sl] * by * bx)
+        t += torch.randn(t.shape, generator=gen, device=device) * 10.0
+        img[sl] = torch.clamp(t, 0.0, 255.0)
+    img_u8 = torch.round(img).to(torch.uint8)
+    del img
+    phi0 = signed_distance_torch(pert_flat.view(Z, Y, X), 3.0)
+    return img_u8, phi0.contiguous(), mask
