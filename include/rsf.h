@@ -153,6 +153,24 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
 rsf_status rsf_set_kernel_timing(rsf_workspace *ws, int enable);
 rsf_status rsf_kernel_times(rsf_workspace *ws, double ms[4], int64_t launches[4], int reset);
 
+/* Evolution without any device allocation, for callers that cannot
+ * allocate once running: work recorded into a CUDA stream capture (an
+ * allocation cannot be captured), plug-ins inside an application that owns
+ * the device memory through its own pool, real-time loops that forbid
+ * allocation after start-up.  Same arguments and result as rsf_evolve, but
+ * no workspace: all scratch lives in one static device array of this
+ * library (about 36 MiB), reserved when its module loads on a device and
+ * held until the process exits.  Limit: W*H*L <= 1048576 voxels; larger
+ * volumes return RSF_ERR_WORKSPACE_TOO_SMALL.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * Every call shares the array and finds the previous call's contents in it;
+ * calls whose work overlaps on one GPU (for instance on two streams) race on
+ * the array and corrupt each other: serialise them.  Non-finite values are
+ * not reported.
+ * This entry point has no counterpart in the reference. */
+rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image, rsf_dtype dtype, float *phi,
+                              int64_t W, int64_t H, int64_t L, int32_t iters, void *stream);
+
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);

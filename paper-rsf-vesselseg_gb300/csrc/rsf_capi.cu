@@ -37,6 +37,8 @@ rsf_status fail(rsf_status s, const char *msg) {
 constexpr int64_t kMaxExtent = 1 << 20;
 }  // namespace
 
+void rsf::set_last_error(const char *msg) { std::snprintf(g_last_error, sizeof g_last_error, "%s", msg); }
+
 struct rsf_workspace {
     int device = -1;
     int64_t max_voxels = 0;

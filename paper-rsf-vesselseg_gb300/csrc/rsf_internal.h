@@ -79,6 +79,9 @@ cudaError_t launch_step(const SubVolDev *d_svs, const int *d_pre, const int *h_t
 
 cudaError_t configure_device();
 
+// Sets the message rsf_last_error() returns on the calling thread.
+void set_last_error(const char *msg);
+
 // Per-kernel launchers; each tap specialisation lives in its own object file.
 #define RSF_DECLARE_K(K)                                                                                      \
     cudaError_t launch_xpass_##K(const SubVolDev *, const int *, int, const StepConst &, int, int, cudaStream_t); \

@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"
 CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in ("xpass", "ypass", "zpass")
              for k in (0, 21, 29, 35)]
             + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
-               ("rsf_capi.cu", "rsf_capi", [])])
+               ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", [])])
 CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp", "sdf.cpp"]
 
 
