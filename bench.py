@@ -213,6 +213,7 @@ def run_ours(args):
     import torch.distributed as dist
 
     from rsf_gb300 import Params, Workspace, synth, tiling
+    from rsf_gb300.dist import max_over_ranks
 
     world, rank, local = dist_env()
     if world > 1:
@@ -267,10 +268,8 @@ def run_ours(args):
     kt = ws.kernel_times(reset=True)
     ws.set_kernel_timing(False)
     ws.check()
+    ms = max_over_ranks(ms, dev)
     if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     vox_iters = total_vox * ITERS * args.steps * world
     value = vox_iters / (ms / 1e3) / 1e9
@@ -312,10 +311,7 @@ def run_ours(args):
     for _ in range(max(1, args.steps // 2)):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dev)
     e2e_value = total_vox * ITERS * world / e2e_s / 1e9
 
     # ---- roofline of the dominant kernel ------------------------------

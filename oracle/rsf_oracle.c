@@ -112,7 +112,7 @@ int oracle_taps(float sigma, float *taps, int cap) {
 /* atan on [-inf, inf] from the identity atan(x) = pi/2 - atan(1/x) (x > 1)   */
 /* and atan(u) = u + u^3 R(u^2) on [0, 1], R a degree-8 polynomial fitted     */
 /* for this project (weighted least squares towards minimax relative error).  */
-/* Max error 0.95 ulp against the exact atan.                                 */
+/* Max error against the exact atan: 0.95 ulp on [-1, 1], 1.35 ulp beyond.   */
 static const float ATAN_R[9] = {
     -0x1.55553e0000000p-2f,
     0x1.9992160000000p-3f,

@@ -16,7 +16,8 @@ namespace rsf {
 enum class Arith : int { Portable = 0, Reference = 1 };
 
 // atan(u) = u + u^3 R(u^2) on [0, 1] with R fitted for this project (degree
-// 8, weighted least squares towards minimax relative error, max 0.95 ulp),
+// 8, weighted least squares towards minimax relative error; max error 0.95
+// ulp on [-1, 1], 1.35 ulp beyond),
 // and atan(x) = pi/2 - atan(1/x) above 1.
 __device__ __forceinline__ float atan_portable(float x) {
     const float a = fabsf(x);

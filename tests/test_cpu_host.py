@@ -1,0 +1,203 @@
+"""CPU tests: the C ABI library loads and exports every declared symbol, its
+host-side helpers, the tiler, the synthetic generator and the multi-process
+helpers (gloo, world size 2).  No device work."""
+import ctypes
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "rsf.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rsf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(rsflib):
+    syms = declared_symbols()
+    assert "rsf_evolve" in syms and "rsf_evolve_batched" in syms and "rsf_status_string" in syms
+    missing = [s for s in syms if not hasattr(rsflib, s)]
+    assert not missing, missing
+
+
+def test_abi_version_and_status_strings(rsflib):
+    assert rsflib.rsf_abi_version() == 1
+    for code in range(11):
+        s = rsflib.rsf_status_string(code)
+        assert s and s != b"unknown status"
+    assert rsflib.rsf_status_string(99) == b"unknown status"
+
+
+def test_params_default_are_reference_cli_defaults(rsflib):
+    from rsf_gb300._lib import RsfParams
+
+    p = RsfParams()
+    assert rsflib.rsf_params_default(ctypes.byref(p)) == 0
+    # CUDA_RSF/main.cpp:91-97 and kernel.cu:258
+    vals = (p.sigma, p.dt, p.mu, p.lambda1, p.lambda2, p.nu, p.eps, p.sigma2)
+    want = (5.0, 0.1, 1.0, 0.1, 0.1, 0.0001, 0.2, 0.0)
+    assert np.allclose(vals, want) and p.boundary == 0 and p.arith == 0
+
+
+@pytest.mark.parametrize("sigma", [0.75, 1.0, 2.5, 3.0, 4.0, 5.0, 10.0])
+def test_taps_identical_to_oracle(rsflib, orc, sigma):
+    from rsf_gb300 import gaussian_taps
+
+    assert np.array_equal(gaussian_taps(sigma), orc.taps(sigma))
+
+
+def test_taps_errors(rsflib):
+    k = ctypes.c_int()
+    assert rsflib.rsf_gaussian_taps(ctypes.c_float(0.0), None, 0, ctypes.byref(k)) == 1
+    assert rsflib.rsf_gaussian_taps(ctypes.c_float(0.6), None, 0, ctypes.byref(k)) == 1
+    assert rsflib.rsf_gaussian_taps(ctypes.c_float(40.0), None, 0, ctypes.byref(k)) == 4
+    buf = (ctypes.c_float * 4)()
+    assert rsflib.rsf_gaussian_taps(ctypes.c_float(3.0), buf, 4, ctypes.byref(k)) == 1
+    assert b"too small" in rsflib.rsf_last_error()
+
+
+def test_workspace_bytes_formula(rsflib):
+    b = rsflib.rsf_workspace_bytes_for(1000, 2)
+    assert b >= 1000 * 36
+
+
+def test_null_arguments_are_rejected_without_device(rsflib):
+    from rsf_gb300._lib import RsfParams
+
+    p = RsfParams()
+    rsflib.rsf_params_default(ctypes.byref(p))
+    assert rsflib.rsf_evolve(None, ctypes.byref(p), None, 0, None, 8, 8, 8, 1, None) == 1
+    assert rsflib.rsf_workspace_destroy(None) == 1
+    assert rsflib.rsf_params_default(None) == 1
+
+
+def test_workspace_create_reports_missing_device(rsflib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert rsflib.rsf_workspace_create(100, 1, ctypes.byref(h)) == 10  # RSF_ERR_NO_DEVICE
+    assert b"no CUDA device" in rsflib.rsf_last_error()
+
+
+# --------------------------------------------------------------------- tiling
+def test_config2_tiles():
+    from rsf_gb300 import tiling
+
+    tiles = tiling.config2_tiles()
+    assert len(tiles) == 48
+    assert sum(t.voxels for t in tiles) == 1216 * 1216 * 640
+    assert {t.shape[0] for t in tiles} == {64, 320, 256}
+    assert {t.shape[1] for t in tiles} == {288, 320} and {t.shape[2] for t in tiles} == {288, 320}
+    cover = np.zeros((512, 1024 // 16, 1024 // 16), dtype=np.int32)  # cores partition the volume
+    for t in tiles:
+        cover[t.clo[0]:t.chi[0], t.clo[1] // 16:t.chi[1] // 16, t.clo[2] // 16:t.chi[2] // 16] += 1
+    assert np.all(cover == 1)
+
+
+def test_plan_cut_reassemble_roundtrip():
+    from rsf_gb300 import tiling
+
+    vol = np.random.default_rng(0).normal(size=(37, 41, 29)).astype(np.float32)
+    tiles = tiling.plan(vol.shape, (10, 16, 7), 3)
+    parts = tiling.cut(vol, tiles)
+    assert all(p.shape == t.shape for p, t in zip(parts, tiles))
+    assert np.array_equal(tiling.reassemble_cores(vol.shape, tiles, parts), vol)
+
+
+def test_blend_halves_matches_interpolating_volumes():
+    """interpolating_volumes.py:10-40: concatenate the non-overlapping parts
+    and blend the overlap with weights linspace(0, 1, overlap) along axis 1."""
+    from rsf_gb300 import tiling
+
+    rng = np.random.default_rng(1)
+    a = rng.normal(size=(5, 30, 7)).astype(np.float32)
+    b = rng.normal(size=(5, 25, 7)).astype(np.float32)
+    ov = 6
+    alpha = np.linspace(0, 1, ov)[None, :, None]
+    want = np.concatenate((a[:, :-ov, :], (1 - alpha) * a[:, -ov:, :] + alpha * b[:, :ov, :], b[:, ov:, :]), axis=1)
+    assert np.allclose(tiling.blend_halves(a, b, ov, axis=1), want)
+
+
+def test_lpt_shards_balance_and_partition():
+    from rsf_gb300 import tiling
+
+    tiles = tiling.config2_tiles()
+    for n in (1, 2, 3, 8):
+        shards = tiling.lpt_shards(tiles, n)
+        assert sorted(i for s in shards for i in s) == list(range(48))
+        loads = [sum(tiles[i].voxels for i in s) for s in shards]
+        assert max(loads) <= 1.2 * sum(loads) / n + max(t.voxels for t in tiles)
+
+
+# ------------------------------------------------------------------ generator
+def test_torch_signed_distance_equals_scipy_edt():
+    import torch
+    from scipy import ndimage
+
+    from rsf_gb300 import synth
+
+    rng = np.random.default_rng(2)
+    m = ndimage.binary_opening(rng.random((24, 27, 25)) < 0.35)
+    got = synth.signed_distance_torch(torch.from_numpy(m), 3.0).numpy()
+    assert np.array_equal(got, synth.signed_distance(m, 3.0))
+
+
+def test_generator_is_seeded_and_in_range():
+    from rsf_gb300 import synth
+
+    a = synth.make_small((20, 22, 24), n_tubes=3, seed=3)
+    b = synth.make_small((20, 22, 24), n_tubes=3, seed=3)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    img, phi0, mask = a
+    assert img.dtype == np.uint8 and phi0.dtype == np.float32 and mask.dtype == bool
+    assert phi0.min() >= -3 and phi0.max() <= 3
+
+
+# ------------------------------------------------------------- multi-process
+def _worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from rsf_gb300 import dist as rd, tiling
+
+    tiles = tiling.config2_tiles()
+    mine = rd.shard(tiles, rank, world)
+    total = rd.sum_over_ranks(len(mine))
+    slowest = rd.max_over_ranks(10.0 + rank)
+    out.put((rank, mine, total, slowest, rd.rank_info()))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_sharding_and_timing_reduction():
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, s0, t0, m0, i0), (r1, s1, t1, m1, i1) = res
+    assert sorted(s0 + s1) == list(range(48)) and not set(s0) & set(s1)
+    assert t0 == t1 == 48
+    assert m0 == m1 == 11.0
+    assert i0 == (2, 0, 0) and i1 == (2, 1, 1)
