@@ -41,6 +41,11 @@
  *
  * The FP64 twin (oracle_evolve_f64) evaluates the same formulas entirely in
  * double; it is used to state the error of the FP32 paths.
+ *
+ * Pinning: every stage is checked bit for bit against the outputs of the
+ * reference's own kernel.cu, compiled unchanged and run on a GB300
+ * (tests/test_reference_kernels.py, fixtures tests/golden/reference_kernels_*.npz);
+ * only H differs, through the reference's single-precision atan.
  */
 #include <math.h>
 #include <stdint.h>
@@ -672,6 +677,12 @@ void oracle_normalise(const float *gx, const float *gy, const float *gz, float *
         nz[i] = normalise_f32(gz[i], m, &d, arith);
     }
 }
+/* Final_phi (kernel.cu:365-387) over arrays, for stage-by-stage checks. */
+void oracle_update_field(const float *phi, const float *dh, const float *eo, const float *ei, const float *kap,
+                         const float *lap, float *out, int64_t n, const oracle_params *p) {
+    for (int64_t i = 0; i < n; i++) out[i] = update_f32(phi[i], dh[i], eo[i], ei[i], kap[i], lap[i], p);
+}
+
 int oracle_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -169,3 +169,24 @@ def atan(x):
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def update_field(phi, dh, eo, ei, kap, lap, p: OracleParams):
+    """Final_phi (kernel.cu:365-387) applied element-wise."""
+    l = lib()
+    if not getattr(l.oracle_update_field, "argtypes", None):
+        l.oracle_update_field.argtypes = [_FP] * 7 + [_I64, ctypes.POINTER(OracleParams)]
+        l.oracle_update_field.restype = None
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (phi, dh, eo, ei, kap, lap)]
+    out = np.empty_like(arrs[0])
+    l.oracle_update_field(*[a.ctypes.data_as(_FP) for a in arrs], out.ctypes.data_as(_FP), out.size, ctypes.byref(p))
+    return out
+
+
+def normalise(gx, gy, gz, form=0, arith=0):
+    """(|g|, nx, ny, nz) as kernel.cu:914-933 and 173-189 compute them."""
+    g = [np.ascontiguousarray(a, dtype=np.float32) for a in (gx, gy, gz)]
+    out = [np.empty_like(g[0]) for _ in range(4)]
+    lib().oracle_normalise(*[a.ctypes.data_as(_FP) for a in g], out[1].ctypes.data_as(_FP), out[2].ctypes.data_as(_FP),
+                           out[3].ctypes.data_as(_FP), out[0].ctypes.data_as(_FP), g[0].size, form, arith)
+    return out
