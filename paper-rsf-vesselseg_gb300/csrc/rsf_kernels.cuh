@@ -187,14 +187,66 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
 // inputs src[i * stride] for i in [0, n), outputs o = i - K + 1 in [0, n-K+1)
 // handed to emit(o, value) as soon as they complete.
 // ---------------------------------------------------------------------------
+// Inputs reach the thread through a private ring of RING float2 slots in
+// shared memory filled by cp.async, so that RING loads per thread are in
+// flight while the multiply-adds run.  Element i lives in slot i % RING and
+// in commit group i; iteration i first refills the slot element i-1 used
+// (with element i-1+RING, group RING+i-1), then waits until at most RING-1
+// groups are pending, which completes group i.
+constexpr int RING = 8;
+
+__device__ __forceinline__ void cp_async8(float2 *smem_dst, const float *gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async4(unsigned *smem_dst, const void *gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_ring() { asm volatile("cp.async.wait_group %0;" ::"n"(RING - 1) : "memory"); }
+
+struct Ring {
+    float2 *base;     // this thread's slot 0; slot s at base + s * step
+    int step;         // threads per block
+    const float *src; // element i at src + i * stride
+    size_t stride;
+    int n;
+    bool act;         // inactive threads load nothing (their results are discarded)
+    // Optional side stream riding in the same commit groups: with element i
+    // comes the aligned 32-bit word holding byte side + (i - lag) * sstride,
+    // for i >= first.  The word around a valid byte stays inside that byte's
+    // 4-byte-aligned block, so it never touches another allocation.
+    unsigned *sbase = nullptr;
+    const unsigned char *side = nullptr;
+    size_t sstride = 0;
+    int lag = 0, first = 0;
+    bool sact = false;
+    __device__ __forceinline__ float2 *slot(int i) const { return base + (i & (RING - 1)) * step; }
+    __device__ __forceinline__ unsigned *sslot(int i) const { return sbase + (i & (RING - 1)) * step; }
+    __device__ __forceinline__ const unsigned char *sbyte(int i) const { return side + (size_t)(i - lag) * sstride; }
+    __device__ __forceinline__ void fill(int i) const {
+        if (act && i < n) {
+            cp_async8(slot(i), src + (size_t)i * stride);
+            if (sact && i >= first)
+                cp_async4(sslot(i), reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(sbyte(i)) & ~(uintptr_t)3));
+        }
+    }
+};
+
 template <int K, bool GUARD, typename Emit>
-__device__ __forceinline__ void stream_block(const float *src, size_t stride, int base, int n, const StepConst &c,
-                                             float2 (&acc)[K], Emit &emit) {
+__device__ __forceinline__ void stream_block(const Ring &rg, int base, const StepConst &c, float2 (&acc)[K],
+                                             Emit &emit) {
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         const int i = base + j;
-        if (GUARD && i >= n) break;
-        const float2 v = ld2(src + (size_t)i * stride);
+        if (GUARD && i >= rg.n) break;
+        if (i > 0) {
+            rg.fill(i - 1 + RING);
+            cp_commit();
+        }
+        cp_wait_ring();
+        const float2 v = *rg.slot(i);
 #pragma unroll
         for (int tt = 0; tt < K; ++tt) {
             const int slot = (j - tt + K) % K;
@@ -202,18 +254,24 @@ __device__ __forceinline__ void stream_block(const float *src, size_t stride, in
             else acc[slot] = fma2(v, c.taps2[tt], acc[slot]);
         }
         const int o = i - (K - 1);
-        if (o >= 0) emit(o, acc[(j + 1) % K]);
+        if (o >= 0) emit(o, acc[(j + 1) % K], i);
     }
 }
 
 template <int K, typename Emit>
-__device__ __forceinline__ void stream_axis(const float *src, size_t stride, int n, const StepConst &c, Emit &emit) {
+__device__ __forceinline__ void stream_axis(const Ring &rg, const StepConst &c, Emit &emit) {
+#pragma unroll
+    for (int q = 0; q < RING; ++q) {
+        rg.fill(q);
+        cp_commit();
+    }
     float2 acc[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] = make_float2(0.f, 0.f);
     int base = 0;
-    for (; base + K <= n; base += K) stream_block<K, false>(src, stride, base, n, c, acc, emit);
-    if (base < n) stream_block<K, true>(src, stride, base, n, c, acc, emit);
+    for (; base + K <= rg.n; base += K) stream_block<K, false>(rg, base, c, acc, emit);
+    if (base < rg.n) stream_block<K, true>(rg, base, c, acc, emit);
+    asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // Register-blocked version for a tap count known only at run time: NB
@@ -249,13 +307,15 @@ __global__ void __launch_bounds__(YP_PAIRS) ypass_kernel(const SubVolDev *__rest
     t /= ntx;
     const int f = t & 3;
     const int z = t >> 2;
+    __shared__ float2 ring[RING * YP_PAIRS];
     const int x = 2 * (tx * YP_PAIRS + threadIdx.x);
     if (x >= s.Wv) return;
     const float *src = s.xb + f * ((size_t)s.Wp * s.H * s.L) + (size_t)z * s.H * s.Wp + x;
     float *dst = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)z * s.Hv * s.Wp + x;
     const size_t wp = (size_t)s.Wp;
-    auto emit = [&](int o, float2 v) { *reinterpret_cast<float2 *>(dst + (size_t)o * wp) = v; };
-    stream_axis<K>(src, wp, s.H, c, emit);
+    auto emit = [&](int o, float2 v, int) { *reinterpret_cast<float2 *>(dst + (size_t)o * wp) = v; };
+    const Ring rg = {ring + threadIdx.x, YP_PAIRS, src, wp, s.H, true};
+    stream_axis<K>(rg, c, emit);
 }
 
 template <int U = 0>
@@ -294,25 +354,23 @@ __global__ void __launch_bounds__(YB_TX) ypass_generic_kernel(const SubVolDev *_
 // its e term; lanes 0 and 2 of the group write lambda (e_out - e_in).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void fits_and_data(const SubVolDev &s, const StepConst &c, int f, int x, int y, int o,
-                                              bool act, float2 B, const DebugOut &dbg, bool debug) {
-    // lane f: 0 -> f_out(x), 1 -> f_in(x), 2 -> f_out(x+1), 3 -> f_in(x+1)
+                                              bool live, float I, float2 B, const DebugOut &dbg, bool debug) {
+    // lane f: 0 -> f_out(x), 1 -> f_in(x), 2 -> f_out(x+1), 3 -> f_in(x+1);
+    // I is the image at that lane's voxel (prefetched by the caller).
     const float bx_hi = __shfl_down_sync(0xffffffffu, B.x, 2);  // lanes 0,1 get IH(x), IHI(x)
     const float by_lo = __shfl_up_sync(0xffffffffu, B.y, 2);    // lanes 2,3 get H(x+1), HI(x+1)
     const float num = f < 2 ? bx_hi : B.y;
     const float den = f < 2 ? B.x : by_lo;
     const float fv = __fdiv_rn(num, den);
     const int xc = x + (f >> 1);
-    const int r = c.r;
-    float I = 0.0f;
-    const size_t vi = ((size_t)(o + r) * s.H + (y + r)) * s.W + (xc + r);
-    const bool live = act && xc < s.Wv;
-    if (live) I = load_img(s.img, vi, c.img_f32);
     const float d = __fsub_rn(I, fv);
     const float e = __fmul_rn(d, d);
     const float e_in = __shfl_down_sync(0xffffffffu, e, 1);  // lanes 0, 2 get e_in of their column
     if (live && (f & 1) == 0)
         s.db[((size_t)o * s.Hv + y) * s.Wp + xc] = data_factor(e, e_in, c.l1, c.l2, c.lam_equal != 0);
     if (debug && live) {
+        const int r = c.r;
+        const size_t vi = ((size_t)(o + r) * s.H + (y + r)) * s.W + (xc + r);
         dbg.f[(size_t)(f & 1) * dbg.n + vi] = fv;
         dbg.f[(size_t)(2 + (f & 1)) * dbg.n + vi] = e;
     }
@@ -334,8 +392,32 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
     const bool act = x < s.Wv;
     const float *src = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)y * s.Wp + (act ? x : 0);
     const size_t pstride = (size_t)s.Wp * s.Hv;
-    auto emit = [&](int o, float2 v) { fits_and_data(s, c, f, x, y, o, act, v, dbg, DEBUG); };
-    stream_axis<K>(src, pstride, s.L, c, emit);
+    __shared__ float2 ring[RING * ZP_PAIRS * 4];
+    __shared__ unsigned iring[RING * ZP_PAIRS * 4];
+    // The image at this lane's voxel of output plane o (input plane o + r)
+    // rides in the ring with element i = o + 2r.
+    const int xc = x + (f >> 1);
+    const bool live = act && xc < s.Wv;
+    const size_t esz = c.img_f32 ? 4 : 1;
+    const unsigned char *img0 = static_cast<const unsigned char *>(s.img) +
+                                (((size_t)(y + c.r)) * s.W + (size_t)(xc + c.r)) * esz;
+    Ring rg = {ring + threadIdx.x, ZP_PAIRS * 4, src, pstride, s.L, act};
+    rg.sbase = iring + threadIdx.x;
+    rg.side = img0;
+    rg.sstride = (size_t)s.W * s.H * esz;
+    rg.lag = c.r;
+    rg.first = 2 * c.r;
+    rg.sact = live;
+    auto emit = [&](int o, float2 v, int i) {
+        float I = 0.0f;
+        if (live) {
+            const unsigned wd = *rg.sslot(i);
+            if (c.img_f32) I = __uint_as_float(wd);
+            else I = (float)((wd >> (8 * (unsigned)(reinterpret_cast<uintptr_t>(rg.sbyte(i)) & 3))) & 0xffu);
+        }
+        fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+    };
+    stream_axis<K>(rg, c, emit);
 }
 
 template <bool DEBUG>
@@ -417,7 +499,7 @@ __device__ __forceinline__ GN gn_from(float xl, float xr, float yl, float yr, fl
 // with the boundary rules of kernel.cu:57-125; used for the previous-row
 // neighbour that x = 0 reads in the reference boundary mode.
 template <Arith A>
-__device__ __noinline__ GN gn_global(const float *__restrict__ phi, int x, int y, int z, int W, int H, int L,
+__device__ __forceinline__ GN gn_global(const float *__restrict__ phi, int x, int y, int z, int W, int H, int L,
                                      int boundary) {
     const size_t WH = (size_t)W * H;
     auto at = [&](int xx, int yy, int zz) { return __ldg(phi + (size_t)zz * WH + (size_t)yy * W + xx); };
@@ -435,6 +517,145 @@ __device__ __noinline__ GN gn_global(const float *__restrict__ phi, int x, int y
     return gn_from<A>(xl, xr, yl, yr, zl, zr);
 }
 
+// Per-block state of the stencil kernel.  Planes are numbered relative to
+// the block's first step; every ring below is indexed by (relative plane mod
+// 3), which the 3-way unrolled step loop turns into compile-time register and
+// shared-memory slots.
+struct StencilCtx {
+    const SubVolDev *s;
+    const float *phi;       // this thread's column of phi (plane 0 at offset 0)
+    float *phi_out;
+    const float *dcol;      // this thread's column of the data factor (plane r)
+    size_t WH, dplane;
+    int W, H, L, r, x, y, w, lane, z0, z1, first;
+    bool in, outp, ref, inside_xy, blk_inside;
+    bool need_x, need_y;
+    ptrdiff_t xoff, yoff;   // offsets of the extra neighbour loads
+    size_t col;
+};
+
+// nx, gx, nz, gz of a plane (ny, gy live in the shared rows)
+struct GN4 {
+    float nx, gx, nz, gz;
+};
+
+struct StencilState {
+    float P[3];     // phi of the planes
+    float EX[3];    // extra x neighbour
+    float EY[3];    // extra y neighbour
+    float DT[3];    // data factor of the planes
+    GN4 G[3];       // gradient / normalised gradient of the planes
+};
+
+__device__ __forceinline__ float st_ld(const StencilCtx &k, int p) {
+    return (k.in && p >= 0 && p < k.L) ? __ldg(k.phi + (size_t)p * k.WH) : 0.0f;
+}
+__device__ __forceinline__ float st_ldx(const StencilCtx &k, int p) {
+    if (!k.need_x || p < 0 || p >= k.L) return 0.0f;
+    // previous linear element of voxel 0 is defined as voxel 0 itself
+    if (k.xoff < 0 && p == 0 && k.col == 0) return __ldg(k.phi);
+    return __ldg(k.phi + (ptrdiff_t)((size_t)p * k.WH) + k.xoff);
+}
+__device__ __forceinline__ float st_ldy(const StencilCtx &k, int p) {
+    return (k.need_y && p >= 0 && p < k.L) ? __ldg(k.phi + (ptrdiff_t)((size_t)p * k.WH) + k.yoff) : 0.0f;
+}
+// data factor at plane p: from the z-pass inside the valid region, from
+// f_out = f_in = 30/30 = 1 in the border band (kernel.cu:300-325).
+__device__ __forceinline__ float st_data(const StencilCtx &k, const StepConst &c, int p) {
+    if (!k.outp || p < k.z0 || p >= k.z1) return 0.0f;
+    if (k.blk_inside || (k.inside_xy && p >= k.r && p < k.L - k.r))
+        return __ldg(k.dcol + (ptrdiff_t)((size_t)p * k.dplane) - (ptrdiff_t)((size_t)k.r * k.dplane));
+    const float I = load_img(k.s->img, (size_t)p * k.WH + k.col, c.img_f32);
+    const float d = __fsub_rn(I, 1.0f);
+    const float e = __fmul_rn(d, d);
+    return data_factor(e, e, c.l1, c.l2, c.lam_equal != 0);
+}
+
+template <int C, Arith A, bool DEBUG>
+__device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepConst &c, StencilState &S, int rel,
+                                             float (*Pb)[ST_WARPS][32], float (*Gb)[2][ST_WARPS][32],
+                                             unsigned *flag, const DebugOut &dbg) {
+    constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
+    const int sc = k.first + rel;  // output plane of this step
+    const int pn = sc + 1;         // plane whose gradient this step computes
+    // prefetch for the next steps
+    const float p3 = st_ld(k, sc + 3);
+    const float exn = st_ldx(k, sc + 3), eyn = st_ldy(k, sc + 3);
+    const float dn = st_data(k, c, sc + 1);
+    Pb[C2][k.w][k.lane] = S.P[C2];
+    const float p0 = S.P[C], p1 = S.P[C1], p2 = S.P[C2];
+    float L1 = __shfl_up_sync(0xffffffffu, p1, 1);
+    float R1 = __shfl_down_sync(0xffffffffu, p1, 1);
+    if (k.need_x && k.xoff < 0) L1 = S.EX[C1];
+    if (k.need_x && k.xoff > 0) R1 = S.EX[C1];
+    const float U1 = k.w > 0 ? Pb[C1][k.w - 1][k.lane] : S.EY[C1];
+    const float D1 = k.w < ST_WARPS - 1 ? Pb[C1][k.w + 1][k.lane] : S.EY[C1];
+    GN gn = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (k.in && pn >= 0 && pn < k.L) {
+        const float xl = (k.x > 0 || k.ref) ? L1 : p1;
+        const float xr = k.x < k.W - 1 ? R1 : p1;
+        const float yl = k.y > 0 ? U1 : p1, yr = k.y < k.H - 1 ? D1 : p1;
+        const float zl = pn > 0 ? p0 : p1, zr = pn < k.L - 1 ? p2 : p1;
+        gn = gn_from<A>(xl, xr, yl, yr, zl, zr);
+    }
+    S.G[C1] = GN4{gn.nx, gn.gx, gn.nz, gn.gz};
+    Gb[C1][0][k.w][k.lane] = gn.ny;
+    Gb[C1][1][k.w][k.lane] = gn.gy;
+    __syncthreads();
+    const GN4 &gc = S.G[C];
+    const float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
+    const float gxL = __shfl_up_sync(0xffffffffu, gc.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gc.gx, 1);
+    if (sc >= k.z0 && k.outp) {
+        float nxl = nxL, gxl = gxL;
+        if (k.x == 0) {
+            if (k.ref && (k.y > 0 || sc > 0)) {
+                const float *phi0 = k.phi - k.col;  // plane 0, voxel 0
+                const GN wg = k.y > 0 ? gn_global<A>(phi0, k.W - 1, k.y - 1, sc, k.W, k.H, k.L, c.boundary)
+                                      : gn_global<A>(phi0, k.W - 1, k.H - 1, sc - 1, k.W, k.H, k.L, c.boundary);
+                nxl = wg.nx;
+                gxl = wg.gx;
+            } else {
+                nxl = gc.nx;
+                gxl = gc.gx;
+            }
+        }
+        const bool xr_in = k.x < k.W - 1;
+        const float nxr = xr_in ? nxR : gc.nx, gxr = xr_in ? gxR : gc.gx;
+        const int wl = k.y > 0 ? k.w - 1 : k.w, wr = k.y < k.H - 1 ? k.w + 1 : k.w;
+        const float nyl = Gb[C][0][wl][k.lane], nyr = Gb[C][0][wr][k.lane];
+        const float gyl = Gb[C][1][wl][k.lane], gyr = Gb[C][1][wr][k.lane];
+        const GN4 &gp = S.G[C2];
+        const float nzl = sc > 0 ? gp.nz : gc.nz, nzr = sc < k.L - 1 ? gn.nz : gc.nz;
+        const float gzl = sc > 0 ? gp.gz : gc.gz, gzr = sc < k.L - 1 ? gn.gz : gc.gz;
+        const float kap = __fadd_rn(__fadd_rn(half_diff(nxr, nxl), half_diff(nyr, nyl)), half_diff(nzr, nzl));
+        const float lap = __fadd_rn(__fadd_rn(half_diff(gxr, gxl), half_diff(gyr, gyl)), half_diff(gzr, gzl));
+        const float dh = dirac<A>(p0, c.eps);
+        const float out = update_phi(p0, dh, S.DT[C], kap, lap, c.dt, c.nu, c.mu);
+        const size_t vi = (size_t)sc * k.WH + k.col;
+        k.phi_out[vi] = out;
+        if (!isfinite(out)) atomicOr(flag, 1u);
+        if constexpr (DEBUG) {
+            const bool inside = k.inside_xy && sc >= k.r && sc < k.L - k.r;
+            if (!inside) {
+                const float I = load_img(k.s->img, vi, c.img_f32);
+                const float d = __fsub_rn(I, 1.0f);
+                dbg.f[0 * dbg.n + vi] = 1.0f;
+                dbg.f[1 * dbg.n + vi] = 1.0f;
+                dbg.f[2 * dbg.n + vi] = __fmul_rn(d, d);
+                dbg.f[3 * dbg.n + vi] = __fmul_rn(d, d);
+            }
+            dbg.f[4 * dbg.n + vi] = dh;
+            dbg.f[5 * dbg.n + vi] = kap;
+            dbg.f[6 * dbg.n + vi] = lap;
+            dbg.f[7 * dbg.n + vi] = grad_mag(gc.gx, Gb[C][1][k.w][k.lane], gc.gz);
+        }
+    }
+    S.P[C] = p3;    // plane rel+3
+    S.EX[C] = exn;  // plane rel+3
+    S.EY[C] = eyn;
+    S.DT[C1] = dn;  // plane rel+1
+}
+
 template <Arith A, bool DEBUG>
 __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolDev *__restrict__ svs,
                                                                    const int *__restrict__ pre,
@@ -445,159 +666,72 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;
     const int sv = find_sv(pre, c.nsv, b);
-    const SubVolDev s = svs[sv];
+    const SubVolDev &s = svs[sv];
     int t = b - __ldg(pre + sv);
-    const int W = s.W, H = s.H, L = s.L;
-    const int ntx = (W + ST_OX - 1) / ST_OX, nty = (H + ST_OY - 1) / ST_OY;
+    StencilCtx k;
+    k.s = &s;
+    k.W = s.W;
+    k.H = s.H;
+    k.L = s.L;
+    k.r = c.r;
+    const int ntx = (k.W + ST_OX - 1) / ST_OX, nty = (k.H + ST_OY - 1) / ST_OY;
     const int tx = t % ntx;
     t /= ntx;
     const int ty = t % nty;
     const int tz = t / nty;
-    const int x = tx * ST_OX - 1 + lane, y = ty * ST_OY - 1 + w;
-    const int z0 = tz * ST_ZC, z1 = min(z0 + ST_ZC, L);
-    const bool in = x >= 0 && x < W && y >= 0 && y < H;
-    const bool outp = in && lane >= 1 && lane <= ST_OX && w >= 1 && w <= ST_OY;
-    const float *__restrict__ phi = parity ? s.phi[1] : s.phi[0];
-    float *__restrict__ phi_out = parity ? s.phi[0] : s.phi[1];
-    const size_t WH = (size_t)W * H;
-    const size_t col = in ? (size_t)y * W + x : 0;
-    const bool ref = c.boundary == 0;
-    const int r = c.r;
-    const bool valid_blur = s.Wv > 0;
+    const int x0 = tx * ST_OX, y0 = ty * ST_OY;
+    k.x = x0 - 1 + lane;
+    k.y = y0 - 1 + w;
+    k.w = w;
+    k.lane = lane;
+    k.z0 = tz * ST_ZC;
+    k.z1 = min(k.z0 + ST_ZC, k.L);
+    k.first = k.z0 - 2;
+    k.in = k.x >= 0 && k.x < k.W && k.y >= 0 && k.y < k.H;
+    k.outp = k.in && lane >= 1 && lane <= ST_OX && w >= 1 && w <= ST_OY;
+    k.ref = c.boundary == 0;
+    k.WH = (size_t)k.W * k.H;
+    k.col = k.in ? (size_t)k.y * k.W + k.x : 0;
+    k.phi = (parity ? s.phi[1] : s.phi[0]) + k.col;
+    k.phi_out = parity ? s.phi[0] : s.phi[1];
+    const bool valid = s.Wv > 0;
+    const int r = k.r;
+    k.inside_xy = valid && k.x >= r && k.x < k.W - r && k.y >= r && k.y < k.H - r;
+    k.blk_inside = valid && x0 >= r && x0 + ST_OX - 1 < k.W - r && y0 >= r && y0 + ST_OY - 1 < k.H - r &&
+                   k.z0 >= r && k.z1 - 1 < k.L - r;
+    k.dplane = (size_t)s.Wp * s.Hv;
+    k.dcol = k.inside_xy ? s.db + (size_t)(k.y - r) * s.Wp + (k.x - r) : s.db;
+    // The shuffles and shared rows supply every neighbour except: x-1 for
+    // lane 0 and, in the reference mode, the previous linear element for
+    // x == 0 (both at linear offset -1); x+1 for lane 31; y-1 / y+1 for the
+    // halo rows.  Corner threads of the halo are never read.
+    const bool halo_row = w == 0 || w == ST_WARPS - 1;
+    const bool halo_col = lane == 0 || lane == 31;
+    k.need_x = k.in && !(halo_row && halo_col) &&
+               ((lane == 0) || (k.x == 0 && k.ref) || (lane == 31 && k.x + 1 < k.W));
+    k.xoff = lane == 31 ? 1 : -1;
+    k.need_y = k.in && halo_row && !halo_col && (w == 0 ? k.y > 0 : k.y + 1 < k.H);
+    k.yoff = w == 0 ? -(ptrdiff_t)k.W : (ptrdiff_t)k.W;
 
-    // Neighbour values the shuffles and shared rows cannot supply:
-    //   x: lane 0 reads x-1; the column x == 0 reads the previous linear
-    //      element in the reference mode; lane 31 reads x+1.
-    //   y: warp 0 reads y-1, the last warp reads y+1.
-    const bool need_xl = in && (lane == 0 || (x == 0 && ref));
-    const bool need_xr = in && lane == 31 && x + 1 < W;
-    const bool need_yl = in && w == 0 && y > 0;
-    const bool need_yr = in && w == ST_WARPS - 1 && y + 1 < H;
-    auto ld = [&](int p) -> float { return (in && p >= 0 && p < L) ? __ldg(phi + (size_t)p * WH + col) : 0.0f; };
-    auto ld_xl = [&](int p) -> float {
-        if (!need_xl || p < 0 || p >= L) return 0.0f;
-        if (x > 0) return __ldg(phi + (size_t)p * WH + col - 1);
-        if (y > 0) return __ldg(phi + (size_t)p * WH + (size_t)(y - 1) * W + (W - 1));
-        if (p > 0) return __ldg(phi + (size_t)(p - 1) * WH + (size_t)(H - 1) * W + (W - 1));
-        return __ldg(phi);
-    };
-    auto ld_xr = [&](int p) -> float {
-        return (need_xr && p >= 0 && p < L) ? __ldg(phi + (size_t)p * WH + col + 1) : 0.0f;
-    };
-    auto ld_y = [&](int p) -> float {
-        if (p < 0 || p >= L) return 0.0f;
-        if (need_yl) return __ldg(phi + (size_t)p * WH + col - W);
-        if (need_yr) return __ldg(phi + (size_t)p * WH + col + W);
-        return 0.0f;
-    };
-    // data factor of (x, y, p): from the z-pass inside the valid region,
-    // f_out = f_in = 30/30 = 1 in the border band.
-    auto ld_data = [&](int p) -> float {
-        if (!outp || p < 0 || p >= L) return 0.0f;
-        const bool inside = valid_blur && x >= r && x < W - r && y >= r && y < H - r && p >= r && p < L - r;
-        if (inside) return __ldg(s.db + ((size_t)(p - r) * s.Hv + (y - r)) * s.Wp + (x - r));
-        const float I = load_img(s.img, (size_t)p * WH + col, c.img_f32);
-        const float d = __fsub_rn(I, 1.0f);
-        const float e = __fmul_rn(d, d);
-        return data_factor(e, e, c.l1, c.l2, c.lam_equal != 0);
-    };
-    auto slot = [](int p) { return (p + 3) % 3; };
-
-    // prologue: planes z0-2, z0-1, z0 in registers, row z0-1 shared
-    const int sp = z0 - 2;
-    float p0 = ld(sp), p1 = ld(sp + 1), p2 = ld(sp + 2);
-    float exl = ld_xl(sp + 1), exr = ld_xr(sp + 1), exy = ld_y(sp + 1);
-    float exl_n = ld_xl(sp + 2), exr_n = ld_xr(sp + 2), exy_n = ld_y(sp + 2);
-    Pb[slot(sp + 1)][w][lane] = p1;
-    GN gprev = {0, 0, 0, 0, 0, 0}, gcur = gprev, gnext = gprev;
-    float dcur = 0.0f;
+    StencilState S;
+    const int sp = k.first;
+    S.P[0] = st_ld(k, sp);
+    S.P[1] = st_ld(k, sp + 1);
+    S.P[2] = st_ld(k, sp + 2);
+    S.EX[1] = st_ldx(k, sp + 1);
+    S.EY[1] = st_ldy(k, sp + 1);
+    S.EX[2] = st_ldx(k, sp + 2);
+    S.EY[2] = st_ldy(k, sp + 2);
+    S.EX[0] = S.EY[0] = 0.0f;
+    S.DT[0] = S.DT[1] = S.DT[2] = 0.0f;
+    for (int i = 0; i < 3; ++i) S.G[i] = GN4{0.f, 0.f, 0.f, 0.f};
+    Pb[1][w][lane] = S.P[1];
     __syncthreads();
-
-    for (int sc = z0 - 2; sc < z1; ++sc) {
-        const int pn = sc + 1;  // plane whose gradient this step computes
-        // prefetch for the next step
-        const float p3 = ld(sc + 3);
-        const float exl_nn = ld_xl(sc + 3), exr_nn = ld_xr(sc + 3), exy_nn = ld_y(sc + 3);
-        const float dnext = (sc + 1 >= z0 && sc + 1 < z1) ? ld_data(sc + 1) : 0.0f;
-        Pb[slot(sc + 2)][w][lane] = p2;
-        // neighbours of plane pn
-        float L1 = __shfl_up_sync(0xffffffffu, p1, 1);
-        float R1 = __shfl_down_sync(0xffffffffu, p1, 1);
-        if (need_xl) L1 = exl;
-        if (lane == 31) R1 = exr;
-        const float U1 = w > 0 ? Pb[slot(pn)][w - 1][lane] : exy;
-        const float D1 = w < ST_WARPS - 1 ? Pb[slot(pn)][w + 1][lane] : exy;
-        if (in && pn >= 0 && pn < L) {
-            const float xl = (x > 0 || ref) ? L1 : p1;
-            const float xr = x < W - 1 ? R1 : p1;
-            const float yl = y > 0 ? U1 : p1, yr = y < H - 1 ? D1 : p1;
-            const float zl = pn > 0 ? p0 : p1, zr = pn < L - 1 ? p2 : p1;
-            gnext = gn_from<A>(xl, xr, yl, yr, zl, zr);
-        } else {
-            gnext = GN{0, 0, 0, 0, 0, 0};
-        }
-        Gb[slot(pn)][0][w][lane] = gnext.ny;
-        Gb[slot(pn)][1][w][lane] = gnext.gy;
-        __syncthreads();
-        // output plane sc
-        const float nxL = __shfl_up_sync(0xffffffffu, gcur.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gcur.nx, 1);
-        const float gxL = __shfl_up_sync(0xffffffffu, gcur.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gcur.gx, 1);
-        if (sc >= z0 && outp) {
-            float nxl = nxL, gxl = gxL;
-            if (x == 0) {
-                if (ref && (y > 0 || sc > 0)) {
-                    const GN wg = y > 0 ? gn_global<A>(phi, W - 1, y - 1, sc, W, H, L, c.boundary)
-                                        : gn_global<A>(phi, W - 1, H - 1, sc - 1, W, H, L, c.boundary);
-                    nxl = wg.nx;
-                    gxl = wg.gx;
-                } else {
-                    nxl = gcur.nx;
-                    gxl = gcur.gx;
-                }
-            }
-            const float nxr = x < W - 1 ? nxR : gcur.nx, gxr = x < W - 1 ? gxR : gcur.gx;
-            const int so = slot(sc);
-            const float nyl = y > 0 ? Gb[so][0][w - 1][lane] : gcur.ny;
-            const float nyr = y < H - 1 ? Gb[so][0][w + 1][lane] : gcur.ny;
-            const float gyl = y > 0 ? Gb[so][1][w - 1][lane] : gcur.gy;
-            const float gyr = y < H - 1 ? Gb[so][1][w + 1][lane] : gcur.gy;
-            const float nzl = sc > 0 ? gprev.nz : gcur.nz, nzr = sc < L - 1 ? gnext.nz : gcur.nz;
-            const float gzl = sc > 0 ? gprev.gz : gcur.gz, gzr = sc < L - 1 ? gnext.gz : gcur.gz;
-            const float kap = __fadd_rn(__fadd_rn(half_diff(nxr, nxl), half_diff(nyr, nyl)), half_diff(nzr, nzl));
-            const float lap = __fadd_rn(__fadd_rn(half_diff(gxr, gxl), half_diff(gyr, gyl)), half_diff(gzr, gzl));
-            const float dh = dirac<A>(p0, c.eps);
-            const float out = update_phi(p0, dh, dcur, kap, lap, c.dt, c.nu, c.mu);
-            const size_t vi = (size_t)sc * WH + col;
-            phi_out[vi] = out;
-            if (!isfinite(out)) atomicOr(flag, 1u);
-            if constexpr (DEBUG) {
-                const bool inside = valid_blur && x >= r && x < W - r && y >= r && y < H - r && sc >= r && sc < L - r;
-                if (!inside) {
-                    const float I = load_img(s.img, vi, c.img_f32);
-                    const float d = __fsub_rn(I, 1.0f);
-                    dbg.f[0 * dbg.n + vi] = 1.0f;
-                    dbg.f[1 * dbg.n + vi] = 1.0f;
-                    dbg.f[2 * dbg.n + vi] = __fmul_rn(d, d);
-                    dbg.f[3 * dbg.n + vi] = __fmul_rn(d, d);
-                }
-                dbg.f[4 * dbg.n + vi] = dh;
-                dbg.f[5 * dbg.n + vi] = kap;
-                dbg.f[6 * dbg.n + vi] = lap;
-                dbg.f[7 * dbg.n + vi] = grad_mag(gcur.gx, gcur.gy, gcur.gz);
-            }
-        }
-        p0 = p1;
-        p1 = p2;
-        p2 = p3;
-        exl = exl_n;
-        exr = exr_n;
-        exy = exy_n;
-        exl_n = exl_nn;
-        exr_n = exr_nn;
-        exy_n = exy_nn;
-        gprev = gcur;
-        gcur = gnext;
-        dcur = dnext;
+    const int count = k.z1 - k.first;
+    for (int i = 0; i < count; i += 3) {
+        stencil_step<0, A, DEBUG>(k, c, S, i, Pb, Gb, flag, dbg);
+        if (i + 1 < count) stencil_step<1, A, DEBUG>(k, c, S, i + 1, Pb, Gb, flag, dbg);
+        if (i + 2 < count) stencil_step<2, A, DEBUG>(k, c, S, i + 2, Pb, Gb, flag, dbg);
     }
 }
 

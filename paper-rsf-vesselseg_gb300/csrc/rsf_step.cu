@@ -58,9 +58,13 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
     const int n1 = c.nsv + 1;
     const int kspec = kernel_k(c.k, arith, dbg != nullptr);
     cudaError_t e = cudaSuccess;
-    // External records so that, inside a stream capture, they become event
-    // record nodes of the graph (a plain record there only orders streams).
-    auto mark = [&](int i) { return ev ? cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal) : cudaSuccess; };
+    // Inside a stream capture a plain record only orders streams; an external
+    // record becomes an event record node of the graph.  Outside a capture
+    // the external flag is not allowed.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (ev && cudaStreamIsCapturing(st, &cap) != cudaSuccess) return cudaGetLastError();
+    const unsigned rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    auto mark = [&](int i) { return ev ? cudaEventRecordWithFlags(ev[i], st, rec_flags) : cudaSuccess; };
     if ((e = mark(0)) != cudaSuccess) return e;
     if (tot[0] > 0) {
         switch (kspec) {
