@@ -138,13 +138,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per voxel of `kernel` from the committed ncu summary."""
-    p = ROOT / "profiles" / "traffic_per_voxel.json"
+def ncu_traffic_ratio(kernel: str):
+    """DRAM bytes / algorithmic bytes of `kernel` in the committed ncu capture
+    (profiles/traffic.json: one launch of a 320^3 volume, larger than L2)."""
+    p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    return d.get("kernels", {}).get(kernel)
+    k = json.loads(p.read_text()).get("kernels", {}).get(kernel)
+    return None if k is None else float(k["ratio"])
 
 
 def cpu_sample(threads: int, budget_s: float = 15.0):
@@ -326,10 +327,12 @@ def run_ours(args):
                          "alg_bytes_per_launch": alg[name], "gbs": alg[name] / (per / 1e3) / 1e9}
     dom = max(kernels, key=lambda n: kernels[n]["ms_per_launch"] * kernels[n]["launches"])
     dk = kernels[dom]
-    tr = ncu_traffic(dom)
+    tr = ncu_traffic_ratio(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": dk["gbs"], "peak": peak, "unit": "GB/s",
                 "frac": dk["gbs"] / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": (tr * total_vox if tr is not None else None),
+                "traffic": (tr * alg[dom] if tr is not None else None),
+                "traffic_source": "ncu DRAM/algorithmic ratio of the same kernel on a 320^3 case "
+                                  "(profiles/traffic.json) times this launch's algorithmic bytes",
                 "step_alg_bytes_per_voxel_iter": sum(alg.values()) / total_vox,
                 "step_gbs": sum(alg.values()) * ITERS * args.steps / (ms / 1e3) / 1e9}
     launches = sum(v[1] for v in kt.values())
