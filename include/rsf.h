@@ -171,6 +171,19 @@ rsf_status rsf_kernel_times(rsf_workspace *ws, double ms[4], int64_t launches[4]
 rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image, rsf_dtype dtype, float *phi,
                               int64_t W, int64_t H, int64_t L, int32_t iters, void *stream);
 
+/* Initial level set from a seed volume (replaces CUDA_RSF/main.cpp:174-183,
+ * which subtracts 13 from the seed and calls tiralib's volume::sdf()).
+ * A voxel is inside when seed > threshold (13 in the reference).  phi
+ * receives the exact signed Euclidean distance in voxels between voxel
+ * centres: +distance to the nearest outside voxel at inside voxels,
+ * -distance to the nearest inside voxel at outside voxels.  When one class
+ * is empty the other is filled with +-(W + H + L).  seed is a device volume
+ * of RSF_U8 or RSF_F32, phi a device float volume of the same shape.
+ * Scratch comes from the workspace (ws must hold >= W*H*L voxels); needs
+ * (W-1)^2 + (H-1)^2 + (L-1)^2 < 2^32 - 1. */
+rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dtype, float threshold, float *phi,
+                               int64_t W, int64_t H, int64_t L, void *stream);
+
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);

@@ -23,6 +23,9 @@
  *   CUDA_RSF/kernel.cu:25-55    Eout_Ein_calculation (box radius (int)sigma2)
  *   CUDA_RSF/kernel.cu:265-280  deri_heaviside delta = (1/pi) eps/(eps^2+phi^2)
  *   CUDA_RSF/kernel.cu:365-387  Final_phi      explicit update
+ *   CUDA_RSF/main.cpp:174-183   phi0 = sdf(seed - 13): this project's own
+ *                               definition (tiralib's sdf is not in the
+ *                               reference), see oracle_signed_distance
  *
  * Arithmetic follows the reference kernels operation by operation.  Every
  * a*b+c that nvcc contracts into a fused multiply-add under its default
@@ -689,4 +692,72 @@ int oracle_max_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/*
+ * Initial level set (CUDA_RSF/main.cpp:174-183: phi0 = sdf(seed - 13)).  The
+ * reference's sdf() is tiralib's (third party, not in the reference
+ * checkout), so this restates the definition the GPU implements, not an
+ * algorithm of the reference: inside = seed > threshold; phi0 = +d(p, outside)
+ * at inside voxels and -d(p, inside) at outside voxels, d Euclidean between
+ * voxel centres; +-(W+H+L) when the other class is empty.  Computed by
+ * direct minimisation: squared distances along x by scanning the row, then
+ * D(y) = min_y' (D(y') + (y-y')^2) over each column and likewise along z, in
+ * exact 64-bit integers (O(n^2) per line: small volumes only).
+ */
+static void sdf_class(const float *seed, float thr, int feat_inside, float *phi, int64_t W, int64_t H,
+                      int64_t L, uint64_t *d, uint64_t *col) {
+    const uint64_t INF = ~(uint64_t)0;
+    for (int64_t z = 0; z < L; z++)
+        for (int64_t y = 0; y < H; y++)
+            for (int64_t x = 0; x < W; x++) {
+                uint64_t best = INF;
+                for (int64_t u = 0; u < W; u++) {
+                    if ((seed[idx3(u, y, z, W, H)] > thr) != (feat_inside != 0)) continue;
+                    uint64_t dd = (uint64_t)((u - x) * (u - x));
+                    if (dd < best) best = dd;
+                }
+                d[idx3(x, y, z, W, H)] = best;
+            }
+    for (int axis = 1; axis <= 2; axis++) {
+        const int64_t n = axis == 1 ? H : L;
+        for (int64_t a = 0; a < (axis == 1 ? L : H); a++)
+            for (int64_t x = 0; x < W; x++) {
+                for (int64_t q = 0; q < n; q++) {
+                    uint64_t best = INF;
+                    for (int64_t v = 0; v < n; v++) {
+                        const uint64_t f = axis == 1 ? d[idx3(x, v, a, W, H)] : d[idx3(x, a, v, W, H)];
+                        if (f == INF) continue;
+                        const uint64_t c = f + (uint64_t)((q - v) * (q - v));
+                        if (c < best) best = c;
+                    }
+                    col[q] = best;
+                }
+                for (int64_t q = 0; q < n; q++) {
+                    if (axis == 1) d[idx3(x, q, a, W, H)] = col[q];
+                    else d[idx3(x, a, q, W, H)] = col[q];
+                }
+            }
+    }
+    const float fill = (float)W + (float)H + (float)L;
+    for (int64_t i = 0; i < W * H * L; i++) {
+        if ((seed[i] > thr) == (feat_inside != 0)) continue;
+        const float mag = d[i] == INF ? fill : sqrtf((float)d[i]);
+        phi[i] = feat_inside ? -mag : mag;
+    }
+}
+
+int oracle_signed_distance(const float *seed, float thr, float *phi, int64_t W, int64_t H, int64_t L) {
+    if (W < 1 || H < 1 || L < 1) return 1;
+    const int64_t n = W * H * L;
+    int64_t m = W > H ? W : H;
+    if (L > m) m = L;
+    uint64_t *d = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    uint64_t *col = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)m);
+    if (!d || !col) { free(d); free(col); return 2; }
+    sdf_class(seed, thr, 0, phi, W, H, L, d, col);
+    sdf_class(seed, thr, 1, phi, W, H, L, d, col);
+    free(d);
+    free(col);
+    return 0;
 }

@@ -190,3 +190,22 @@ def normalise(gx, gy, gz, form=0, arith=0):
     lib().oracle_normalise(*[a.ctypes.data_as(_FP) for a in g], out[1].ctypes.data_as(_FP), out[2].ctypes.data_as(_FP),
                            out[3].ctypes.data_as(_FP), out[0].ctypes.data_as(_FP), g[0].size, form, arith)
     return out
+
+
+def signed_distance(seed, threshold: float = 13.0) -> np.ndarray:
+    """phi0 of CUDA_RSF/main.cpp:174-183 as this project defines it: exact
+    signed Euclidean distance of {seed > threshold}, positive inside.  Brute
+    force per line, small volumes only.  Parity of this definition with the
+    reference's tiralib sdf() is unpinned (tiralib is not in the reference)."""
+    s = np.ascontiguousarray(seed, dtype=np.float32)
+    if s.ndim != 3:
+        raise ValueError("seed must be 3-D (L, H, W)")
+    L, H, W = s.shape
+    out = np.empty_like(s)
+    l = lib()
+    if not getattr(l.oracle_signed_distance, "argtypes", None):
+        l.oracle_signed_distance.argtypes = [_FP, ctypes.c_float, _FP, _I64, _I64, _I64]
+    rc = l.oracle_signed_distance(s.ctypes.data_as(_FP), threshold, out.ctypes.data_as(_FP), W, H, L)
+    if rc:
+        raise RuntimeError(f"oracle_signed_distance failed ({rc})")
+    return out

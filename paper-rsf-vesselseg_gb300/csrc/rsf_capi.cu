@@ -504,6 +504,24 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");
 }
 
+// CUDA_RSF/main.cpp:174-183: phi0 = sdf(seed - 13).  The transform is defined
+// in rsf_sdf.cu; scratch is the x-field pool (12 of its 16 bytes per voxel).
+rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dtype, float threshold, float *phi,
+                               int64_t W, int64_t H, int64_t L, void *stream) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    if (!seed || !phi) return fail(RSF_ERR_INVALID_ARGUMENT, "seed and phi must be device pointers");
+    if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "seed dtype must be RSF_U8 or RSF_F32");
+    if (W < 1 || H < 1 || L < 1) return fail(RSF_ERR_SHAPE, "W, H and L must be >= 1");
+    if (W > 32768 || H > 32768 || L > 32768) return fail(RSF_ERR_SHAPE, "extents above 32768 are not supported");
+    const uint64_t dmax = (uint64_t)(W - 1) * (W - 1) + (uint64_t)(H - 1) * (H - 1) + (uint64_t)(L - 1) * (L - 1);
+    if (dmax >= 0xffffffffull) return fail(RSF_ERR_SHAPE, "squared diagonal exceeds 32 bits");
+    if (W * H * L > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "volume larger than the workspace");
+    cudaError_t e = rsf::launch_signed_distance(seed, dtype == RSF_F32, threshold, phi, (int)W, (int)H, (int)L,
+                                                reinterpret_cast<unsigned *>(ws->pool_x), (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "signed distance launch");
+    return RSF_OK;
+}
+
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
     cudaStream_t st = (cudaStream_t)stream;

@@ -96,5 +96,8 @@ RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
                            unsigned *flag, const DebugOut *dbg, cudaStream_t);
+// Signed distance of {seed > thr}; scratch holds 3 * W*H*L words.
+cudaError_t launch_signed_distance(const void *seed, int f32, float thr, float *phi, int W, int H, int L,
+                                   unsigned *scratch, cudaStream_t st);
 
 }  // namespace rsf

@@ -127,6 +127,24 @@ class Workspace:
                                    ctypes.c_void_p(_stream_ptr(stream))))
         return phi
 
+    def signed_distance(self, seed, threshold: float = 13.0, out=None, stream=None):
+        """phi0 from a seed volume (CUDA_RSF/main.cpp:174-183): the exact signed
+        Euclidean distance of {seed > threshold}, positive inside.  `seed` is a
+        uint8 or float32 CUDA tensor (L, H, W); returns `out` (float32)."""
+        import torch
+        _require_cuda(seed)
+        if seed.dim() != 3:
+            raise ValueError("seed must be 3-D (L, H, W)")
+        seed = seed.contiguous()
+        if out is None:
+            out = torch.empty(seed.shape, dtype=torch.float32, device=seed.device)
+        _require_cuda(out)
+        L, H, W = seed.shape
+        check(self._lib.rsf_signed_distance(self.handle, ctypes.c_void_p(seed.data_ptr()), _dtype_code(seed.dtype),
+                                            ctypes.c_float(threshold), ctypes.c_void_p(out.data_ptr()), W, H, L,
+                                            ctypes.c_void_p(_stream_ptr(stream))))
+        return out
+
     def evolve_batched(self, pairs, params: Params, iters: int, stream=None):
         """Evolves a list of (image, phi) CUDA tensor pairs, each phi in place."""
         if not pairs:

@@ -29,8 +29,9 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"
 CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in ("xpass", "ypass", "zpass")
              for k in (0, 21, 29, 35)]
             + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
-               ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", [])])
-CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp", "sdf.cpp"]
+               ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", []),
+               ("rsf_sdf.cu", "rsf_sdf", [])])
+CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp"]
 
 
 def nvcc() -> str:
@@ -78,7 +79,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         cli_objs.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC,
-                         "-c", CSRC / src, "-o", obj])
+                         "-I", Path(nv).resolve().parents[1] / "include", "-c", CSRC / src, "-o", obj])
     outputs = []
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for res in ex.map(lambda c: _run(c, verbose), jobs):
@@ -89,7 +90,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     if force or _stale(LIB_PATH, objs):
         _run([nv, *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcudart"], verbose)
     if cli_objs and (force or _stale(CLI_PATH, cli_objs + [LIB_PATH])):
-        _run(["g++", "-o", CLI_PATH, *cli_objs, f"-L{LIB_DIR}", "-lrsf_gb300", f"-Wl,-rpath,{LIB_DIR}",
+        _run(["g++", "-o", CLI_PATH, *cli_objs, f"-L{LIB_DIR}", "-lrsf_gb300", "-Wl,-rpath,$ORIGIN/../lib",
               f"-L{Path(nv).resolve().parents[1] / 'lib64'}", "-lcudart"], verbose)
     return LIB_PATH
 

@@ -1,0 +1,125 @@
+"""CPU checks of the initial level set (oracle) and of the rsf3d front end.
+
+The signed distance restated in the oracle is compared with SciPy's exact
+Euclidean distance transform; the command-line tool is checked for the
+reference's option handling (CUDA_RSF/main.cpp:86-110) up to the point where
+it needs a device.
+"""
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import PKG
+
+CLI = PKG / "bin" / "rsf3d"
+
+
+def _scipy_sdf(seed, thr):
+    from scipy import ndimage
+
+    m = seed > thr
+    if m.all() or not m.any():
+        L, H, W = seed.shape
+        return np.full(seed.shape, (1.0 if m.all() else -1.0) * (W + H + L), dtype=np.float32)
+    return np.where(m, ndimage.distance_transform_edt(m), -ndimage.distance_transform_edt(~m)).astype(np.float32)
+
+
+def _blobs(shape, seed):
+    from scipy import ndimage
+
+    rng = np.random.default_rng(seed)
+    return ndimage.uniform_filter((rng.random(shape) * 30).astype(np.float32), 3)
+
+
+@pytest.mark.parametrize("shape", [(9, 11, 13), (1, 1, 7), (7, 1, 1), (1, 9, 1), (6, 7, 1), (12, 10, 14), (2, 3, 33)])
+def test_oracle_sdf_equals_scipy_edt(orc, shape):
+    seed = _blobs(shape, sum(shape))
+    thr = float(np.median(seed))
+    got = orc.signed_distance(seed, thr)
+    assert np.array_equal(got.view(np.uint32), _scipy_sdf(seed, thr).view(np.uint32))
+
+
+def test_oracle_sdf_one_class_fill_and_threshold_strictness(orc):
+    seed = np.full((4, 5, 6), 13.0, dtype=np.float32)
+    # seed == threshold is outside: the reference's sdf(seed - 13) sees 0 there
+    assert np.all(orc.signed_distance(seed, 13.0) == -15.0)
+    assert np.all(orc.signed_distance(seed, 12.5) == 15.0)
+    seed[2, 2, 3] = 20.0
+    phi = orc.signed_distance(seed, 13.0)
+    assert phi[2, 2, 3] == 1.0
+    assert phi[0, 0, 0] == -np.float32(np.sqrt(4 + 4 + 9))
+
+
+def test_oracle_sdf_is_a_distance_field(orc):
+    seed = _blobs((16, 18, 20), 3)
+    phi = orc.signed_distance(seed, float(np.median(seed)))
+    # 1-Lipschitz along each axis between voxels of one class
+    for ax in range(3):
+        d = np.abs(np.diff(phi.astype(np.float64), axis=ax))
+        same = np.sign(np.take(phi, range(phi.shape[ax] - 1), axis=ax)) == np.sign(
+            np.take(phi, range(1, phi.shape[ax]), axis=ax))
+        assert d[same].max() <= 1.0 + 1e-6
+    assert np.all(np.abs(phi) >= 1.0)
+
+
+def _cli():
+    from rsf_gb300 import build
+
+    build.build()
+    assert CLI.exists()
+    return str(CLI)
+
+
+def _run(*args):
+    return subprocess.run([_cli(), *args], capture_output=True, text=True, timeout=60)
+
+
+def test_cli_help_lists_reference_options_and_exits_1():
+    r = _run("--help")
+    assert r.returncode == 1
+    for name in ("sigma", "t", "dt", "meu", "e", "v", "sigma2", "binary", "image", "ouput", "debug"):
+        assert f"--{name} " in r.stdout or f"--{name}\n" in r.stdout
+    assert "--sigma arg (=5)" in r.stdout and "--t arg (=30)" in r.stdout and "--ouput arg (=out.npy)" in r.stdout
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["--s", "3"], "ambiguous"),
+    (["--bogus", "1"], "unrecognised"),
+    (["--sigma"], "needs a value"),
+    (["--debug=1"], "takes no value"),
+    (["-t", "3"], "unexpected argument"),
+    (["--sigma", "x3"], "malformed"),
+    (["--boundary", "wrap", "--image", "a", "--binary", "b"], "--boundary"),
+    (["--t", "3"], "--image and --binary are required"),
+])
+def test_cli_usage_errors_exit_2(args, msg):
+    r = _run(*args)
+    assert r.returncode == 2, r.stderr
+    assert msg in r.stderr
+
+
+def test_cli_prefixes_and_output_alias_parse(tmp_path):
+    # unambiguous prefixes resolve (--me -> --meu, --ou -> --ouput/--output);
+    # the run then stops at the missing input file, before any device work
+    r = _run("--me", "1", "--ou", str(tmp_path / "o.npy"), "--bin", str(tmp_path / "none.npy"), "--ima",
+             str(tmp_path / "none2.npy"))
+    assert r.returncode == 3 and "cannot open" in r.stderr
+
+
+def test_cli_npy_reader_rejects_bad_files_and_shape_mismatch(tmp_path):
+    img = tmp_path / "img.npy"
+    seed = tmp_path / "seed.npy"
+    np.save(img, np.zeros((4, 5, 6), dtype=np.uint8))
+    np.save(seed, np.zeros((4, 5, 7), dtype=np.float32))
+    r = _run("--image", str(img), "--binary", str(seed))
+    assert r.returncode == 3 and "differ in shape" in r.stderr
+    np.save(seed, np.zeros((4, 5), dtype=np.float32))
+    r = _run("--image", str(img), "--binary", str(seed))
+    assert r.returncode == 3 and "3-D" in r.stderr
+    (tmp_path / "junk.npy").write_bytes(b"not an array")
+    r = _run("--image", str(img), "--binary", str(tmp_path / "junk.npy"))
+    assert r.returncode == 3 and "not a .npy" in r.stderr
+    np.save(seed, np.zeros((4, 5, 6), dtype=np.complex64))
+    r = _run("--image", str(img), "--binary", str(seed))
+    assert r.returncode == 3 and "unsupported dtype" in r.stderr
