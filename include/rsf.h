@@ -184,6 +184,23 @@ rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image, rsf_dtype 
 rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dtype, float threshold, float *phi,
                                int64_t W, int64_t H, int64_t L, void *stream);
 
+/* Reverse-mode derivative of one evolution step phi -> phi' (the step of
+ * CUDA_RSF/main.cpp:233-300; no counterpart in the reference, which has no
+ * derivative).  Given phi (the state before the step) and phi_bar_in =
+ * dL/dphi', writes phi_bar_out = dL/dphi and, when param_grads is not NULL,
+ * ADDS dL/dlambda1, dL/dlambda2, dL/dmu, dL/dnu to param_grads[0..3] (device
+ * doubles), so a chain of calls sums them over the steps.  The data term is
+ * differentiated as lambda1 e_out - lambda2 e_in with both weights
+ * independent (for tied weights add the two).  The derivative is that of the
+ * real-valued step evaluated in FP32 (p->arith is ignored); sigma2 >= 1 is
+ * RSF_ERR_UNSUPPORTED as in the forward.  phi_bar_out must not overlap phi,
+ * phi_bar_in or the image.  Scratch comes from the workspace (ws must hold
+ * >= W*H*L voxels); parameter sums use atomics, so their last bits may vary
+ * from run to run. */
+rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
+                            const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
+                            int64_t W, int64_t H, int64_t L, void *stream);
+
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);

@@ -522,6 +522,36 @@ rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dt
     return RSF_OK;
 }
 
+// The derivative of one step; kernels and the chain rule are in rsf_adjoint.cu.
+rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
+                            const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
+                            int64_t W, int64_t H, int64_t L, void *stream) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    float taps[rsf::MAXK];
+    int k = 0;
+    rsf_status s = check_params(p, &k, taps);
+    if (s != RSF_OK) return s;
+    if ((s = check_shape(W, H, L)) != RSF_OK) return s;
+    if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
+    if (!image || !phi || !phi_bar_in || !phi_bar_out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
+    const int64_t n = W * H * L;
+    if (n > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "volume larger than the workspace");
+    auto overlaps = [n](const void *a, size_t abytes, const void *b) {
+        const char *pa = static_cast<const char *>(a), *pb = static_cast<const char *>(b);
+        return pa < pb + n * sizeof(float) && pb < pa + abytes;
+    };
+    const size_t img_bytes = (size_t)n * (dtype == RSF_F32 ? 4 : 1);
+    if (overlaps(phi_bar_out, n * sizeof(float), phi) || overlaps(phi_bar_out, n * sizeof(float), phi_bar_in) ||
+        overlaps(image, img_bytes, phi_bar_out))
+        return fail(RSF_ERR_INVALID_ARGUMENT, "phi_bar_out overlaps an input");
+    cudaError_t e = rsf::launch_step_adjoint(taps, k, p->eps, p->dt, p->mu, p->nu, p->lambda1, p->lambda2,
+                                             p->boundary, dtype == RSF_F32, phi, image, phi_bar_in, phi_bar_out,
+                                             param_grads, (int)W, (int)H, (int)L, ws->pool_phi2, ws->pool_x,
+                                             ws->pool_y, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    return RSF_OK;
+}
+
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
     cudaStream_t st = (cudaStream_t)stream;

@@ -96,6 +96,12 @@ RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
                            unsigned *flag, const DebugOut *dbg, cudaStream_t);
+// Reverse-mode derivative of one step (rsf_adjoint.cu); scratch from the
+// workspace pools phi2 (N floats), xs (4N) and ys (4N).
+cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,
+                                int boundary, int img_f32, const float *phi, const void *img, const float *u,
+                                float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
+                                cudaStream_t st);
 // Signed distance of {seed > thr}; scratch holds 3 * W*H*L words.
 cudaError_t launch_signed_distance(const void *seed, int f32, float thr, float *phi, int W, int H, int L,
                                    unsigned *scratch, cudaStream_t st);

@@ -61,6 +61,8 @@ SIGNATURES = {
                                       _P]),
     "rsf_workspace_check": (ctypes.c_int, [_P, _P]),
     "rsf_signed_distance": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_float, _P, _I64, _I64, _I64, _P]),
+    "rsf_step_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), _P, ctypes.c_int, _P, _P, _P, _P, _I64, _I64,
+                                        _I64, _P]),
     "rsf_set_kernel_timing": (ctypes.c_int, [_P, ctypes.c_int]),
     "rsf_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                         ctypes.c_int]),

@@ -145,6 +145,28 @@ class Workspace:
                                             ctypes.c_void_p(_stream_ptr(stream))))
         return out
 
+    def step_adjoint(self, image, phi, phi_bar, params: Params, out=None, param_grads=None, stream=None):
+        """dL/dphi of one step phi -> phi' given phi_bar = dL/dphi'.  When
+        `param_grads` (CUDA float64, 4 elements) is given, dL/d(lambda1,
+        lambda2, mu, nu) are added to it.  Returns `out` (new if None)."""
+        import torch
+        _require_cuda(image, phi, phi_bar)
+        L, H, W = phi.shape
+        if out is None:
+            out = torch.empty_like(phi)
+        _require_cuda(out)
+        gp = None
+        if param_grads is not None:
+            _require_cuda(param_grads)
+            if param_grads.dtype != torch.float64 or param_grads.numel() < 4:
+                raise TypeError("param_grads must be a CUDA float64 tensor of 4 elements")
+            gp = ctypes.c_void_p(param_grads.data_ptr())
+        check(self._lib.rsf_step_adjoint(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image.data_ptr()),
+                                         _dtype_code(image.dtype), ctypes.c_void_p(phi.data_ptr()),
+                                         ctypes.c_void_p(phi_bar.data_ptr()), ctypes.c_void_p(out.data_ptr()), gp,
+                                         W, H, L, ctypes.c_void_p(_stream_ptr(stream))))
+        return out
+
     def evolve_batched(self, pairs, params: Params, iters: int, stream=None):
         """Evolves a list of (image, phi) CUDA tensor pairs, each phi in place."""
         if not pairs:

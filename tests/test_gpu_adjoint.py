@@ -1,0 +1,166 @@
+"""GPU checks of the hand-written adjoint (rsf_step_adjoint) and of the
+checkpointed torch.autograd.Function built on it.
+
+Checkers: the float64 autograd restatement (oracle/rsf_autograd.py) for
+vector-Jacobian products of one step and of whole evolutions, and FP64
+central differences of the C oracle for the 50-step, checkpoint-every-10
+case.  The adjoint runs in FP32, so the bars are relative: 1e-4 (L2 norm) for
+one step, 1e-3 for chains, as the gradient tolerance of the benchmark spec states.
+"""
+import numpy as np
+import pytest
+
+from test_adjoint_ref_cpu import PP, f32, smooth_case, soft_dice_np
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _params(**kw):
+    from rsf_gb300 import Params
+
+    d = dict(PP)
+    d.update(kw)
+    return Params(**{k: d[k] for k in ("sigma", "dt", "mu", "lambda1", "lambda2", "nu", "eps")},
+                  sigma2=d.get("sigma2", 0.0), boundary=d.get("boundary", "reference"))
+
+
+def _rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def _vjp_fp64(orc, phi, img, u, p, boundary):
+    from oracle import rsf_autograd as ra
+
+    step = ra.Step(phi.shape, orc.taps(p.sigma), f32(p.dt), f32(p.eps), 0 if boundary == "reference" else 1)
+    x = torch.from_numpy(phi.astype(np.float64)).requires_grad_(True)
+    prm = {k: torch.tensor(f32(getattr(p, k)), dtype=torch.float64, requires_grad=True)
+           for k in ("lambda1", "lambda2", "mu", "nu")}
+    out = step(x, torch.from_numpy(img.astype(np.float64)), prm["lambda1"], prm["lambda2"], prm["mu"], prm["nu"])
+    (out * torch.from_numpy(u.astype(np.float64))).sum().backward()
+    return x.grad.numpy(), np.array([prm[k].grad.item() for k in ("lambda1", "lambda2", "mu", "nu")])
+
+
+STEP_CASES = [
+    ((16, 18, 20), 1.5, "reference", "smooth", "f32"),
+    ((16, 18, 20), 1.5, "clamp", "smooth", "f32"),
+    ((24, 20, 30), 1.0, "reference", "sdf3", "u8"),
+    ((9, 8, 10), 1.5, "reference", "smooth", "f32"),  # 11 taps: no valid blur region
+    ((2, 3, 40), 1.0, "reference", "smooth", "f32"),
+    ((40, 24, 26), 3.0, "reference", "smooth", "u8"),
+]
+
+
+@pytest.mark.parametrize("shape,sigma,boundary,kind,dt", STEP_CASES)
+def test_single_step_adjoint_matches_fp64_autograd(ws_big, orc, shape, sigma, boundary, kind, dt):
+    from rsf_gb300 import synth
+
+    rng = np.random.default_rng(sum(shape))
+    img, phi, mask = smooth_case(shape)
+    if kind == "sdf3":  # clipped signed distance: flat regions where g = 0 exactly
+        phi = synth.signed_distance(mask, clip=3.0)
+    if dt == "u8":
+        img_dev = torch.from_numpy(np.round(img * 255).astype(np.uint8)).cuda()
+        img_ref = np.round(img * 255).astype(np.float32)
+        p = _params(sigma=sigma, boundary=boundary, lambda1=1e-4, lambda2=2e-4)
+    else:
+        img_dev = torch.from_numpy(img).cuda()
+        img_ref = img
+        p = _params(sigma=sigma, boundary=boundary, lambda2=0.7)
+    u = rng.standard_normal(shape).astype(np.float32)
+    g = torch.zeros(4, dtype=torch.float64, device="cuda")
+    got = ws_big.step_adjoint(img_dev, torch.from_numpy(phi).cuda(), torch.from_numpy(u).cuda(), p,
+                              param_grads=g).cpu().numpy()
+    want, want_p = _vjp_fp64(orc, phi, img_ref, u, p, boundary)
+    assert _rel(got, want) <= 1e-4
+    gp = g.cpu().numpy()
+    for k in range(4):
+        assert abs(gp[k] - want_p[k]) <= 1e-4 * max(abs(want_p[k]), 1e-3 * np.abs(want_p).max()), k
+
+
+def _grads_gpu(img, phi0, mask, p, T, every):
+    from rsf_gb300 import autograd
+
+    prm = {k: torch.tensor(f32(getattr(p, k)), dtype=torch.float64, device="cuda", requires_grad=True)
+           for k in ("lambda1", "lambda2", "mu", "nu")}
+    x = torch.from_numpy(phi0).cuda().requires_grad_(True)
+    phiT = autograd.evolve(x, torch.from_numpy(img).cuda(), p, T, checkpoint_every=every, **prm)
+    loss = autograd.soft_dice_loss(phiT.double(), torch.from_numpy(mask).cuda(), p.eps)
+    loss.backward()
+    return x.grad.cpu().numpy(), np.array([prm[k].grad.item() for k in ("lambda1", "lambda2", "mu", "nu")])
+
+
+def test_checkpointed_chain_matches_fp64_autograd(cuda, rsflib, orc):
+    from oracle import rsf_autograd as ra
+
+    shape, T = (20, 22, 24), 12
+    img, phi0, mask = smooth_case(shape)
+    p = _params(lambda2=0.8)
+    got, got_p = _grads_gpu(img, phi0, mask, p, T, 5)
+    x = torch.from_numpy(phi0.astype(np.float64)).requires_grad_(True)
+    prm = {k: torch.tensor(f32(getattr(p, k)), dtype=torch.float64, requires_grad=True)
+           for k in ("lambda1", "lambda2", "mu", "nu")}
+    phiT = ra.evolve(x, torch.from_numpy(img.astype(np.float64)), orc.taps(p.sigma),
+                     dict(dt=f32(p.dt), eps=f32(p.eps), **prm), T)
+    from rsf_gb300 import autograd
+
+    autograd.soft_dice_loss(phiT, torch.from_numpy(mask), p.eps).backward()
+    assert _rel(got, x.grad.numpy()) <= 1e-3
+    for k, name in enumerate(("lambda1", "lambda2", "mu", "nu")):
+        assert abs(got_p[k] - prm[name].grad.item()) <= 1e-3 * abs(prm[name].grad.item()), name
+
+
+def test_checkpoint_interval_does_not_change_the_gradient(cuda, rsflib):
+    shape, T = (16, 18, 20), 7
+    img, phi0, mask = smooth_case(shape, seed=5)
+    p = _params()
+    ref, ref_p = _grads_gpu(img, phi0, mask, p, T, T)
+    for every in (1, 3):
+        got, got_p = _grads_gpu(img, phi0, mask, p, T, every)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))  # recompute is bit-identical
+        assert np.allclose(got_p, ref_p, rtol=1e-9, atol=0)
+
+
+def test_fifty_steps_every_ten_against_fp64_central_differences(cuda, rsflib, orc):
+    """The differentiable workload at reduced size: T = 50, checkpoints every
+    10, soft-Dice loss, FP64 central differences with h = 1e-4."""
+    from scipy import ndimage
+
+    shape, T = (40, 40, 40), 50
+    img, phi0, mask = smooth_case(shape, seed=11)
+    p = _params()
+    got, got_p = _grads_gpu(img, phi0, mask, p, T, 10)
+
+    def loss(phi0_, **kw):
+        P = orc.params(**dict(PP, **kw))
+        return soft_dice_np(orc.evolve_f64(phi0_.astype(np.float64), img, P, T), mask)
+
+    for seed in (1, 2):
+        v = ndimage.gaussian_filter(np.random.default_rng(seed).standard_normal(shape), 2.0)
+        v /= np.abs(v).max()
+        h = 1e-4
+        fd = (loss(phi0 + h * v) - loss(phi0 - h * v)) / (2 * h)
+        ad = float((got.astype(np.float64) * v).sum())
+        assert abs(ad - fd) <= 1e-3 * abs(fd), (ad, fd)
+    for k, name in enumerate(("lambda1", "lambda2", "mu", "nu")):
+        base = PP[name]
+        up, dn = f32(base * (1 + 1e-3)), f32(base * (1 - 1e-3))
+        fd = (loss(phi0, **{name: up}) - loss(phi0, **{name: dn})) / (up - dn)
+        assert abs(got_p[k] - fd) <= 1e-3 * abs(fd), (name, got_p[k], fd)
+
+
+def test_adjoint_argument_errors(cuda, rsflib):
+    from rsf_gb300 import RsfError, Workspace
+
+    img = torch.rand((10, 10, 10), device=cuda)
+    phi = torch.rand((10, 10, 10), device=cuda)
+    u = torch.rand((10, 10, 10), device=cuda)
+    with Workspace(1000) as ws:
+        with pytest.raises(RsfError):
+            ws.step_adjoint(img, phi, u, _params(), out=u)  # output overlaps an input
+        with pytest.raises(RsfError):
+            ws.step_adjoint(img, phi, u, _params(sigma2=1.0))
+    with Workspace(999) as ws:
+        with pytest.raises(RsfError):
+            ws.step_adjoint(img, phi, u, _params())
