@@ -90,6 +90,19 @@ typedef struct {
     int64_t W, H, L;
 } rsf_subvol;
 
+/* One evolved sub-volume placed in a larger volume (rsf_reassemble). */
+typedef struct {
+    const float *phi;     /* W*H*L float32, device */
+    int64_t x0, y0, z0;   /* position of its first voxel in the output */
+    int64_t W, H, L;
+} rsf_tile;
+
+/* Stitching modes of rsf_reassemble. */
+typedef enum {
+    RSF_REASSEMBLE_CORE = 0,  /* each voxel from the sub-volume whose core holds it */
+    RSF_REASSEMBLE_BLEND = 1  /* linear blend across overlaps */
+} rsf_reassemble_mode;
+
 typedef struct rsf_workspace rsf_workspace;
 
 /* Library identification. */
@@ -200,6 +213,22 @@ rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dt
 rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
                             const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
                             int64_t W, int64_t H, int64_t L, void *stream);
+
+/* Stitches a grid of evolved sub-volumes into `out` (W*H*L float32, device),
+ * the step of the reference's missing reassemble.py (README.md:9) and of
+ * interpolating_volumes.py:10-40.  Core boundaries core_x[0..nx] (0 .. W),
+ * core_y[0..ny], core_z[0..nz] partition the volume; tiles[(iz*ny + iy)*nx +
+ * ix] holds cell (ix, iy, iz), must contain its core box and must share its
+ * x extent with every tile of index ix (likewise y, z).  RSF_REASSEMBLE_CORE
+ * copies each core; RSF_REASSEMBLE_BLEND weights each tile, per axis, by a
+ * ramp rising from 0 to 1 in equal steps across its overlap with the
+ * previous tile and falling across its overlap with the next (the weights of
+ * interpolating_volumes.py), multiplies the axes and normalises.  At most
+ * 64 cells per axis and max_subvols tiles; the tile table travels through
+ * the workspace. */
+rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, int32_t ny, int32_t nz,
+                          const int64_t *core_x, const int64_t *core_y, const int64_t *core_z, int32_t mode,
+                          float *out, int64_t W, int64_t H, int64_t L, void *stream);
 
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */

@@ -552,6 +552,73 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
     return RSF_OK;
 }
 
+// Grid checks on the host; the gather itself is in rsf_reassemble.cu.  The
+// tile table goes through the workspace's pinned staging and device table.
+rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, int32_t ny, int32_t nz,
+                          const int64_t *core_x, const int64_t *core_y, const int64_t *core_z, int32_t mode,
+                          float *out, int64_t W, int64_t H, int64_t L, void *stream) {
+    static_assert(sizeof(rsf::TileDev) <= sizeof(SubVolDev), "tile table must fit the sub-volume table");
+    if (!ws || !tiles || !core_x || !core_y || !core_z || !out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
+    if (mode != RSF_REASSEMBLE_CORE && mode != RSF_REASSEMBLE_BLEND)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "unknown reassembly mode");
+    const int n[3] = {nx, ny, nz};
+    const int64_t ext[3] = {W, H, L};
+    const int64_t *core[3] = {core_x, core_y, core_z};
+    for (int a = 0; a < 3; a++) {
+        if (n[a] < 1 || n[a] > rsf::RA_MAXCELLS) return fail(RSF_ERR_INVALID_ARGUMENT, "1 to 64 cells per axis");
+        if (ext[a] < 1 || ext[a] > kMaxExtent) return fail(RSF_ERR_SHAPE, "bad output extent");
+        if (core[a][0] != 0 || core[a][n[a]] != ext[a]) return fail(RSF_ERR_INVALID_ARGUMENT, "cores must span the volume");
+        for (int j = 0; j < n[a]; j++)
+            if (core[a][j] >= core[a][j + 1]) return fail(RSF_ERR_INVALID_ARGUMENT, "core bounds must increase");
+    }
+    const int64_t ntiles = (int64_t)nx * ny * nz;
+    if (ntiles > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more tiles than the workspace holds");
+    int cb[3][rsf::RA_MAXCELLS + 1], lo[3][rsf::RA_MAXCELLS], hi[3][rsf::RA_MAXCELLS];
+    for (int a = 0; a < 3; a++) {
+        for (int j = 0; j <= n[a]; j++) cb[a][j] = (int)core[a][j];
+        for (int j = 0; j < n[a]; j++) lo[a][j] = hi[a][j] = -1;
+    }
+    if (ws->table_pending) {
+        cudaError_t e = cudaEventSynchronize(ws->table_ev);
+        if (e != cudaSuccess) return cuda_fail(e, "table event");
+        ws->table_pending = false;
+    }
+    rsf::TileDev *h = reinterpret_cast<rsf::TileDev *>(ws->h_svs);
+    for (int iz = 0; iz < nz; iz++)
+        for (int iy = 0; iy < ny; iy++)
+            for (int ix = 0; ix < nx; ix++) {
+                const int64_t t = ((int64_t)iz * ny + iy) * nx + ix;
+                const rsf_tile &s = tiles[t];
+                const int idx[3] = {ix, iy, iz};
+                const int64_t o[3] = {s.x0, s.y0, s.z0}, e[3] = {s.W, s.H, s.L};
+                if (!s.phi) return fail(RSF_ERR_INVALID_ARGUMENT, "null tile pointer");
+                for (int a = 0; a < 3; a++) {
+                    const int j = idx[a];
+                    if (e[a] < 1 || o[a] < 0 || o[a] + e[a] > ext[a])
+                        return fail(RSF_ERR_SHAPE, "tile extends outside the volume");
+                    if (o[a] > core[a][j] || o[a] + e[a] < core[a][j + 1])
+                        return fail(RSF_ERR_INVALID_ARGUMENT, "tile does not contain its core");
+                    if (lo[a][j] < 0) {
+                        lo[a][j] = (int)o[a];
+                        hi[a][j] = (int)(o[a] + e[a]);
+                    } else if (lo[a][j] != (int)o[a] || hi[a][j] != (int)(o[a] + e[a])) {
+                        return fail(RSF_ERR_INVALID_ARGUMENT, "tiles of one grid row must share their extent");
+                    }
+                }
+                h[t] = rsf::TileDev{s.phi, (int)s.x0, (int)s.y0, (int)s.z0, (int)s.W, (int)s.H, (int)s.L};
+            }
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(ws->d_svs, h, (size_t)ntiles * sizeof(rsf::TileDev), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ws->table_ev, st);
+    if (e != cudaSuccess) return cuda_fail(e, "tile table upload");
+    ws->table_pending = true;
+    const int *pcb[3] = {cb[0], cb[1], cb[2]}, *plo[3] = {lo[0], lo[1], lo[2]}, *phi_[3] = {hi[0], hi[1], hi[2]};
+    e = rsf::launch_reassemble(reinterpret_cast<const rsf::TileDev *>(ws->d_svs), n, pcb, plo, phi_, mode, out,
+                               (int)W, (int)H, (int)L, st);
+    if (e != cudaSuccess) return cuda_fail(e, "reassembly launch");
+    return RSF_OK;
+}
+
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
     cudaStream_t st = (cudaStream_t)stream;

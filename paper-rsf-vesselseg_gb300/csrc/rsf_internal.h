@@ -102,6 +102,15 @@ cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, f
                                 int boundary, int img_f32, const float *phi, const void *img, const float *u,
                                 float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
                                 cudaStream_t st);
+// Reassembly (rsf_reassemble.cu): one evolved sub-volume placed in the output.
+constexpr int RA_MAXCELLS = 64;  // grid cells per axis
+struct TileDev {
+    const float *phi;
+    int x0, y0, z0;
+    int W, H, L;
+};
+cudaError_t launch_reassemble(const TileDev *d_tiles, const int n[3], const int *const cb[3], const int *const lo[3],
+                              const int *const hi[3], int mode, float *out, int W, int H, int L, cudaStream_t st);
 // Signed distance of {seed > thr}; scratch holds 3 * W*H*L words.
 cudaError_t launch_signed_distance(const void *seed, int f32, float thr, float *phi, int W, int H, int L,
                                    unsigned *scratch, cudaStream_t st);

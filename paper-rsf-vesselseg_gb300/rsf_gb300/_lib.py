@@ -32,6 +32,11 @@ class RsfSubvol(ctypes.Structure):
                 ("H", ctypes.c_int64), ("L", ctypes.c_int64)]
 
 
+class RsfTile(ctypes.Structure):
+    _fields_ = [("phi", ctypes.c_void_p), ("x0", ctypes.c_int64), ("y0", ctypes.c_int64), ("z0", ctypes.c_int64),
+                ("W", ctypes.c_int64), ("H", ctypes.c_int64), ("L", ctypes.c_int64)]
+
+
 class RsfError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
@@ -61,6 +66,7 @@ SIGNATURES = {
                                       _P]),
     "rsf_workspace_check": (ctypes.c_int, [_P, _P]),
     "rsf_signed_distance": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_float, _P, _I64, _I64, _I64, _P]),
+    "rsf_reassemble": (ctypes.c_int, [_P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P, _I64, _I64, _I64, _P]),
     "rsf_step_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), _P, ctypes.c_int, _P, _P, _P, _P, _I64, _I64,
                                         _I64, _P]),
     "rsf_set_kernel_timing": (ctypes.c_int, [_P, ctypes.c_int]),

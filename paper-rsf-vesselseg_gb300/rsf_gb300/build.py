@@ -30,7 +30,8 @@ CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in (
              for k in (0, 21, 29, 35)]
             + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
                ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", []),
-               ("rsf_sdf.cu", "rsf_sdf", []), ("rsf_adjoint.cu", "rsf_adjoint", [])])
+               ("rsf_sdf.cu", "rsf_sdf", []), ("rsf_adjoint.cu", "rsf_adjoint", []),
+               ("rsf_reassemble.cu", "rsf_reassemble", [])])
 CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp"]
 
 

@@ -108,27 +108,46 @@ def cut(volume: np.ndarray, tiles: Sequence[Tile]):
     return [np.ascontiguousarray(volume[t.slices()]) for t in tiles]
 
 
-def reassemble_cores(shape, tiles: Sequence[Tile], parts, dtype=np.float32) -> np.ndarray:
-    """Writes every tile's core region into a full volume (core crop)."""
-    out = np.empty(shape, dtype=dtype)
-    for t, p in zip(tiles, parts):
-        out[t.core_slices()] = np.asarray(p)[t.core_in_tile()]
+def grid_bounds(tiles: Sequence[Tile]):
+    """Core boundaries per axis (z, y, x) of a tile grid as `plan` makes it,
+    checking that the tiles are listed z-major, then y, then x."""
+    bounds = [sorted({t.clo[a] for t in tiles} | {t.chi[a] for t in tiles}) for a in range(3)]
+    n = [len(b) - 1 for b in bounds]
+    if n[0] * n[1] * n[2] != len(tiles):
+        raise ValueError("tiles do not form a grid")
+    for i, t in enumerate(tiles):
+        iz, iy, ix = i // (n[1] * n[2]), (i // n[2]) % n[1], i % n[2]
+        if (t.clo, t.chi) != ((bounds[0][iz], bounds[1][iy], bounds[2][ix]),
+                              (bounds[0][iz + 1], bounds[1][iy + 1], bounds[2][ix + 1])):
+            raise ValueError("tiles are not in grid order (z-major, then y, then x)")
+    return bounds
+
+
+def reassemble_device(ws, tiles: Sequence[Tile], parts, shape, mode: str = "core", out=None, stream=None):
+    """Stitches evolved tiles (CUDA float32 tensors, one per tile, in `plan`
+    order) into `out` (CUDA float32, `shape` = (L, H, W)) on the device with
+    rsf_reassemble: "core" copies each tile's core, "blend" blends linearly
+    across the overlaps (interpolating_volumes.py:10-40 generalised to a grid)."""
+    import ctypes
+
+    import torch
+
+    from . import _lib
+    from .api import _stream_ptr
+
+    bz, by, bx = grid_bounds(tiles)
+    if out is None:
+        out = torch.empty(tuple(shape), dtype=torch.float32, device=parts[0].device)
+    arr = (_lib.RsfTile * len(tiles))()
+    for i, (t, p) in enumerate(zip(tiles, parts)):
+        if tuple(p.shape) != t.shape or p.dtype != torch.float32 or not p.is_cuda or not p.is_contiguous():
+            raise TypeError(f"part {i} must be a contiguous CUDA float32 tensor of shape {t.shape}")
+        arr[i] = _lib.RsfTile(p.data_ptr(), t.lo[2], t.lo[1], t.lo[0], t.shape[2], t.shape[1], t.shape[0])
+    cx = (ctypes.c_int64 * len(bx))(*bx)
+    cy = (ctypes.c_int64 * len(by))(*by)
+    cz = (ctypes.c_int64 * len(bz))(*bz)
+    L, H, W = shape
+    _lib.check(ws._lib.rsf_reassemble(ws.handle, arr, len(bx) - 1, len(by) - 1, len(bz) - 1, cx, cy, cz,
+                                      {"core": 0, "blend": 1}[mode], ctypes.c_void_p(out.data_ptr()), W, H, L,
+                                      ctypes.c_void_p(_stream_ptr(stream))))
     return out
-
-
-def blend_halves(a: np.ndarray, b: np.ndarray, overlap: int, axis: int = 1) -> np.ndarray:
-    """Linear blend of two volumes that overlap by `overlap` voxels along
-    `axis`: the weight of `b` rises from 0 to 1 across the overlap (the
-    behaviour of interpolating_volumes.py:10-40, which blends along axis 1)."""
-    if overlap < 1:
-        return np.concatenate([a, b], axis=axis)
-    w = np.linspace(0.0, 1.0, overlap)
-    shape = [1] * a.ndim
-    shape[axis] = overlap
-    w = w.reshape(shape)
-    a_keep = np.take(a, range(a.shape[axis] - overlap), axis=axis)
-    b_keep = np.take(b, range(overlap, b.shape[axis]), axis=axis)
-    a_ov = np.take(a, range(a.shape[axis] - overlap, a.shape[axis]), axis=axis)
-    b_ov = np.take(b, range(overlap), axis=axis)
-    mid = (1.0 - w) * a_ov + w * b_ov
-    return np.concatenate([a_keep, mid, b_keep], axis=axis)

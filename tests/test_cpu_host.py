@@ -108,7 +108,9 @@ def test_plan_cut_reassemble_roundtrip():
     tiles = tiling.plan(vol.shape, (10, 16, 7), 3)
     parts = tiling.cut(vol, tiles)
     assert all(p.shape == t.shape for p, t in zip(parts, tiles))
-    assert np.array_equal(tiling.reassemble_cores(vol.shape, tiles, parts), vol)
+    from oracle import reassembly
+
+    assert np.array_equal(reassembly.reassemble_cores(vol.shape, tiles, parts), vol)
 
 
 def test_blend_halves_matches_interpolating_volumes():
@@ -122,7 +124,9 @@ def test_blend_halves_matches_interpolating_volumes():
     ov = 6
     alpha = np.linspace(0, 1, ov)[None, :, None]
     want = np.concatenate((a[:, :-ov, :], (1 - alpha) * a[:, -ov:, :] + alpha * b[:, :ov, :], b[:, ov:, :]), axis=1)
-    assert np.allclose(tiling.blend_halves(a, b, ov, axis=1), want)
+    from oracle import reassembly
+
+    assert np.allclose(reassembly.blend_halves(a, b, ov, axis=1), want)
 
 
 def test_lpt_shards_balance_and_partition():
@@ -201,3 +205,32 @@ def test_two_rank_sharding_and_timing_reduction():
     assert t0 == t1 == 48
     assert m0 == m1 == 11.0
     assert i0 == (2, 0, 0) and i1 == (2, 1, 1)
+
+
+def test_grid_blend_of_two_tiles_is_the_reference_blend():
+    from oracle import reassembly
+    from rsf_gb300 import tiling
+
+    tiles = [tiling.Tile((0, 0, 0), (6, 30, 5), (0, 0, 0), (6, 20, 5)),
+             tiling.Tile((0, 10, 0), (6, 50, 5), (0, 20, 0), (6, 50, 5))]
+    rng = np.random.default_rng(0)
+    a, b = rng.standard_normal(tiles[0].shape), rng.standard_normal(tiles[1].shape)
+    got = reassembly.blend_grid((6, 50, 5), tiles, [a, b])
+    assert np.allclose(got, reassembly.blend_halves(a, b, 20, axis=1), rtol=0, atol=1e-12)
+
+
+def test_grid_bounds_and_chunking():
+    from rsf_gb300 import driver, tiling
+
+    tiles = tiling.plan((40, 48, 56), ([0, 8, 30, 40], 16, [0, 20, 56]), 5)
+    bz, by, bx = tiling.grid_bounds(tiles)
+    assert bz == [0, 8, 30, 40] and by == [0, 16, 32, 48] and bx == [0, 20, 56]
+    with pytest.raises(ValueError):
+        tiling.grid_bounds(tiles[::-1])
+    with pytest.raises(ValueError):
+        tiling.grid_bounds(tiles[:-1])
+    groups = driver.chunk_tiles(tiles, 20000)
+    assert sorted(i for g in groups for i in g) == list(range(len(tiles)))
+    for g in groups:
+        assert len(g) == 1 or sum(tiles[i].voxels for i in g) <= 20000
+        assert g == list(range(g[0], g[-1] + 1))
