@@ -77,7 +77,7 @@ typedef struct {
     float lambda2;  /* --e 0.1: weight of e_in */
     float nu;       /* --v 1e-4: curvature (length) weight */
     float eps;      /* 0.2: Heaviside/Dirac width, hard-coded in kernel.cu:258,275 */
-    float sigma2;   /* --sigma2 0.0: (int) radius of the e-term box window */
+    float sigma2;   /* --sigma2 0.0: (int) radius of the e-term box window, 0..8 */
     int32_t boundary; /* rsf_boundary */
     int32_t arith;    /* rsf_arith */
     int32_t reserved[6];
@@ -205,8 +205,8 @@ rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dt
  * doubles), so a chain of calls sums them over the steps.  The data term is
  * differentiated as lambda1 e_out - lambda2 e_in with both weights
  * independent (for tied weights add the two).  The derivative is that of the
- * real-valued step evaluated in FP32 (p->arith is ignored); sigma2 >= 1 is
- * RSF_ERR_UNSUPPORTED as in the forward.  phi_bar_out must not overlap phi,
+ * real-valued step evaluated in FP32 (p->arith is ignored); the box e-term
+ * (sigma2 >= 1) has no adjoint here (RSF_ERR_UNSUPPORTED).  phi_bar_out must not overlap phi,
  * phi_bar_in or the image.  Scratch comes from the workspace (ws must hold
  * >= W*H*L voxels); parameter sums use atomics, so their last bits may vary
  * from run to run. */

@@ -680,6 +680,11 @@ void oracle_normalise(const float *gx, const float *gy, const float *gz, float *
         nz[i] = normalise_f32(gz[i], m, &d, arith);
     }
 }
+/* Eout_Ein_calculation (kernel.cu:25-55) over given fits, box radius s. */
+void oracle_data_terms(const float *I, const float *fo, const float *fi, float *eo, float *ei, int64_t W, int64_t H,
+                       int64_t L, int s) {
+    data_terms(I, fo, fi, eo, ei, W, H, L, s);
+}
 /* Final_phi (kernel.cu:365-387) over arrays, for stage-by-stage checks. */
 void oracle_update_field(const float *phi, const float *dh, const float *eo, const float *ei, const float *kap,
                          const float *lap, float *out, int64_t n, const oracle_params *p) {

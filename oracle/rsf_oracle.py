@@ -209,3 +209,16 @@ def signed_distance(seed, threshold: float = 13.0) -> np.ndarray:
     if rc:
         raise RuntimeError(f"oracle_signed_distance failed ({rc})")
     return out
+
+
+def data_terms(I, fo, fi, s: int):
+    """(e_out, e_in) of kernel.cu:25-55 for given fits and box radius s."""
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (I, fo, fi)]
+    L, H, W = a[0].shape
+    eo, ei = np.empty_like(a[0]), np.empty_like(a[0])
+    l = lib()
+    if not getattr(l.oracle_data_terms, "argtypes", None):
+        l.oracle_data_terms.argtypes = [_FP] * 5 + [_I64, _I64, _I64, ctypes.c_int]
+    l.oracle_data_terms(*[x.ctypes.data_as(_FP) for x in a], eo.ctypes.data_as(_FP), ei.ctypes.data_as(_FP),
+                        W, H, L, int(s))
+    return eo, ei

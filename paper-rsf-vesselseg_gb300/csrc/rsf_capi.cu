@@ -220,7 +220,7 @@ rsf_status check_params(const rsf_params *p, int *k, float *taps) {
         if (!std::isfinite(v)) return fail(RSF_ERR_INVALID_ARGUMENT, "non-finite parameter");
     if (!(p->eps > 0.0f)) return fail(RSF_ERR_INVALID_ARGUMENT, "eps must be > 0");
     if (p->sigma2 < 0.0f) return fail(RSF_ERR_INVALID_ARGUMENT, "sigma2 must be >= 0");
-    if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "box e-term (sigma2 >= 1) is not implemented on the GPU");
+    if (p->sigma2 >= (float)(rsf::MAX_BOX + 1)) return fail(RSF_ERR_UNSUPPORTED, "sigma2 above 8 is not supported");
     if (p->boundary != RSF_BOUNDARY_REFERENCE && p->boundary != RSF_BOUNDARY_CLAMP)
         return fail(RSF_ERR_INVALID_ARGUMENT, "unknown boundary mode");
     if (p->arith != RSF_ARITH_PORTABLE && p->arith != RSF_ARITH_REFERENCE)
@@ -321,6 +321,7 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
     c.xb_w = xb_w;
+    c.box = (int)p->sigma2;
     return c;
 }
 
@@ -381,7 +382,7 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
     int tot[rsf::NKERN], xb_w = 0;
-    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false), dtype, nullptr, tot, &xb_w, st);
+    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), dtype, nullptr, tot, &xb_w, st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
     const StepConst c = make_const(p, k, taps, dtype, n, xb_w);
@@ -532,6 +533,7 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
     if ((s = check_shape(W, H, L)) != RSF_OK) return s;
+    if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the box e-term (sigma2 >= 1) is not implemented");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
     if (!image || !phi || !phi_bar_in || !phi_bar_out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
     const int64_t n = W * H * L;

@@ -41,7 +41,7 @@ const Option kOptions[] = {
     {"meu", true, "1", "weight for the regularization term"},
     {"e", true, "0.1", "weight for the fitting term (lambda1 = lambda2 = e)"},
     {"v", true, "0.0001", "weight for the smoothing term"},
-    {"sigma2", true, "0", "weight for sigma2 (box radius of the e-term; only 0 is supported)"},
+    {"sigma2", true, "0", "weight for sigma2 (box radius (int)sigma2 of the e-term, 0..8)"},
     {"binary", true, nullptr, "binary seed surface (.npy)"},
     {"image", true, nullptr, "input image filename (.npy)"},
     {"ouput", true, "out.npy", "output level set (.npy)"},

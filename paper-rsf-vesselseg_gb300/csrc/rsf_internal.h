@@ -28,6 +28,9 @@ constexpr int XB_CHOICES[2] = {5, 9};
 //   yb: 4 y-pass fields, each Wp x Hv x L
 //   db: data factor lambda (e_out - e_in) of the valid region, Wp x Hv x Lv;
 //       it reuses the x-pass storage, which is dead once the y-pass has run.
+//       With the box e-term it holds f_out and f_in of the valid region
+//       (Wp x Hv x Lv each) followed by the data factor of every voxel
+//       (W x H x L).
 struct SubVolDev {
     float *phi[2];       // ping-pong level-set buffers
     const void *img;     // image, uint8 or float32
@@ -51,6 +54,7 @@ struct StepConst {
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
     int xb_w;       // x-pass outputs per lane for this launch
+    int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
 };
 
 // Optional per-voxel debug outputs (8 fields, full-volume layout).
@@ -62,9 +66,13 @@ struct DebugOut {
 constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil
 
 // Tap counts with streaming (compile-time K) kernels.  Other tap counts, the
-// debug step and the reference arithmetic use the run-time-k kernels.
+// debug step, the reference arithmetic and the box e-term use the
+// run-time-k kernels.
 inline bool is_specialised(int k) { return k == 21 || k == 29 || k == 35; }
-inline int kernel_k(int k, int arith, bool debug) { return (is_specialised(k) && arith == 0 && !debug) ? k : 0; }
+inline int kernel_k(int k, int arith, bool debug, int box = 0) {
+    return (is_specialised(k) && arith == 0 && !debug && box == 0) ? k : 0;
+}
+constexpr int MAX_BOX = 8;  // largest e-term box radius
 
 // Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
 void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]);
@@ -96,6 +104,8 @@ RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
                            unsigned *flag, const DebugOut *dbg, cudaStream_t);
+// Box e-term (c.box >= 1): data factor of every voxel, stencil tiling.
+cudaError_t launch_box(const SubVolDev *, const int *, int, const StepConst &, const DebugOut *dbg, cudaStream_t);
 // Reverse-mode derivative of one step (rsf_adjoint.cu); scratch from the
 // workspace pools phi2 (N floats), xs (4N) and ys (4N).
 cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,

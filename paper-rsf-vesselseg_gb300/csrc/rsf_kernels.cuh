@@ -456,6 +456,16 @@ __global__ void __launch_bounds__(ZB_TX) zpass_generic_kernel(const SubVolDev *_
         const int o = z0 + m;
         if (o >= s.Lv) break;
         const size_t vi = ((size_t)(o + r) * s.H + (y + r)) * s.W + (x + r);
+        if (c.box > 0) {  // the box kernel forms e from the fits
+            const size_t di = ((size_t)o * s.Hv + y) * s.Wp + x;
+            s.db[di] = fo[m];
+            s.db[(size_t)s.Wp * s.Hv * s.Lv + di] = fi[m];
+            if (DEBUG) {
+                dbg.f[0 * dbg.n + vi] = fo[m];
+                dbg.f[1 * dbg.n + vi] = fi[m];
+            }
+            continue;
+        }
         const float I = load_img(s.img, vi, c.img_f32);
         const float d_o = __fsub_rn(I, fo[m]), d_i = __fsub_rn(I, fi[m]);
         const float eo = __fmul_rn(d_o, d_o), ei = __fmul_rn(d_i, d_i);
@@ -637,12 +647,14 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
         if constexpr (DEBUG) {
             const bool inside = k.inside_xy && sc >= k.r && sc < k.L - k.r;
             if (!inside) {
-                const float I = load_img(k.s->img, vi, c.img_f32);
-                const float d = __fsub_rn(I, 1.0f);
                 dbg.f[0 * dbg.n + vi] = 1.0f;
                 dbg.f[1 * dbg.n + vi] = 1.0f;
-                dbg.f[2 * dbg.n + vi] = __fmul_rn(d, d);
-                dbg.f[3 * dbg.n + vi] = __fmul_rn(d, d);
+                if (c.box == 0) {  // the box kernel wrote e everywhere
+                    const float I = load_img(k.s->img, vi, c.img_f32);
+                    const float d = __fsub_rn(I, 1.0f);
+                    dbg.f[2 * dbg.n + vi] = __fmul_rn(d, d);
+                    dbg.f[3 * dbg.n + vi] = __fmul_rn(d, d);
+                }
             }
             dbg.f[4 * dbg.n + vi] = dh;
             dbg.f[5 * dbg.n + vi] = kap;
@@ -654,6 +666,70 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
     S.EX[C] = exn;  // plane rel+3
     S.EY[C] = eyn;
     S.DT[C1] = dn;  // plane rel+1
+}
+
+// ---------------------------------------------------------------------------
+// Box e-term, CUDA_RSF/kernel.cu:25-55 with s = (int)sigma2 >= 1: for every
+// voxel c, e = sum over the neighbours n of the (2s+1)^3 box that lie inside
+// the volume of w (I_n - f(c))^2, w = 1/(2s+1)^2, accumulated in the
+// reference's order (y outer, then x, then z) with each term fused in double
+// and rounded to float.  f(c) comes from the z-pass in the valid region and
+// is 30/30 = 1 in the border band.  Writes the data factor of every voxel;
+// runs on the stencil's tiling (lanes 1..30 x warps 1..14 x 32 planes).
+// ---------------------------------------------------------------------------
+template <bool DEBUG>
+__global__ void __launch_bounds__(ST_WARPS * 32) box_kernel(const SubVolDev *__restrict__ svs,
+                                                            const int *__restrict__ pre, const StepConst c,
+                                                            DebugOut dbg) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int b = blockIdx.x;
+    const int sv = find_sv(pre, c.nsv, b);
+    const SubVolDev &s = svs[sv];
+    int t = b - __ldg(pre + sv);
+    const int ntx = (s.W + ST_OX - 1) / ST_OX, nty = (s.H + ST_OY - 1) / ST_OY;
+    const int tx = t % ntx;
+    t /= ntx;
+    const int ty = t % nty;
+    const int tz = t / nty;
+    const int x = tx * ST_OX - 1 + lane, y = ty * ST_OY - 1 + w;
+    if (lane < 1 || lane > ST_OX || w < 1 || w > ST_OY || x >= s.W || y >= s.H) return;
+    const int z0 = tz * ST_ZC, z1 = min(z0 + ST_ZC, s.L);
+    const int bs = c.box, r = c.r;
+    const double wt = 1.0 / (double)((2 * bs + 1) * (2 * bs + 1));
+    const size_t WH = (size_t)s.W * s.H, nvalid = (size_t)s.Wp * s.Hv * s.Lv;
+    float *dfull = s.db + 2 * nvalid;
+    const bool valid_xy = s.Wv > 0 && x >= r && x < r + s.Wv && y >= r && y < r + s.Hv;
+    for (int z = z0; z < z1; ++z) {
+        float fo = 1.0f, fi = 1.0f;
+        if (valid_xy && z >= r && z < r + s.Lv) {
+            const size_t di = ((size_t)(z - r) * s.Hv + (y - r)) * s.Wp + (x - r);
+            fo = s.db[di];
+            fi = s.db[nvalid + di];
+        }
+        float s1 = 0.0f, s2 = 0.0f;
+        for (int u = -bs; u <= bs; ++u) {
+            const int yy = y + u;
+            if (yy < 0 || yy >= s.H) continue;
+            for (int v = -bs; v <= bs; ++v) {
+                const int xx = x + v;
+                if (xx < 0 || xx >= s.W) continue;
+                for (int q = -bs; q <= bs; ++q) {
+                    const int zz = z + q;
+                    if (zz < 0 || zz >= s.L) continue;
+                    const float In = load_img(s.img, (size_t)zz * WH + (size_t)yy * s.W + xx, c.img_f32);
+                    const float d1 = __fsub_rn(In, fo), d2 = __fsub_rn(In, fi);
+                    s1 = __double2float_rn(__fma_rn(__dmul_rn(wt, (double)d1), (double)d1, (double)s1));
+                    s2 = __double2float_rn(__fma_rn(__dmul_rn(wt, (double)d2), (double)d2, (double)s2));
+                }
+            }
+        }
+        const size_t vi = (size_t)z * WH + (size_t)y * s.W + x;
+        dfull[vi] = data_factor(s1, s2, c.l1, c.l2, c.lam_equal != 0);
+        if (DEBUG) {
+            dbg.f[2 * dbg.n + vi] = s1;
+            dbg.f[3 * dbg.n + vi] = s2;
+        }
+    }
 }
 
 template <Arith A, bool DEBUG>
@@ -701,6 +777,11 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
                    k.z0 >= r && k.z1 - 1 < k.L - r;
     k.dplane = (size_t)s.Wp * s.Hv;
     k.dcol = k.inside_xy ? s.db + (size_t)(k.y - r) * s.Wp + (k.x - r) : s.db;
+    if (c.box > 0) {  // every voxel's data factor comes from the box kernel
+        k.blk_inside = true;
+        k.dplane = k.WH;
+        k.dcol = s.db + 2 * (size_t)s.Wp * s.Hv * s.Lv + k.col + (size_t)r * k.WH;
+    }
     // The shuffles and shared rows supply every neighbour except: x-1 for
     // lane 0 and, in the reference mode, the previous linear element for
     // x == 0 (both at linear offset -1); x+1 for lane 31; y-1 / y+1 for the

@@ -17,4 +17,12 @@ cudaError_t launch_stencil(const SubVolDev *svs, const int *pre, int blocks, con
     return cudaGetLastError();
 }
 
+cudaError_t launch_box(const SubVolDev *svs, const int *pre, int blocks, const StepConst &c, const DebugOut *dbg,
+                       cudaStream_t st) {
+    constexpr int T = ST_WARPS * 32;
+    if (dbg) box_kernel<true><<<blocks, T, 0, st>>>(svs, pre, c, *dbg);
+    else box_kernel<false><<<blocks, T, 0, st>>>(svs, pre, c, DebugOut{nullptr, 0});
+    return cudaGetLastError();
+}
+
 }  // namespace rsf

@@ -56,7 +56,7 @@ cudaError_t configure_device() {
 cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, const StepConst &c, int parity,
                         int arith, unsigned *flag, const DebugOut *dbg, cudaStream_t st, cudaEvent_t *ev) {
     const int n1 = c.nsv + 1;
-    const int kspec = kernel_k(c.k, arith, dbg != nullptr);
+    const int kspec = kernel_k(c.k, arith, dbg != nullptr, c.box);
     cudaError_t e = cudaSuccess;
     // Inside a stream capture a plain record only orders streams; an external
     // record becomes an event record node of the graph.  Outside a capture
@@ -93,6 +93,10 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
             case 35: e = launch_zpass_35(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
             default: e = launch_zpass_0(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
         }
+        if (e != cudaSuccess) return e;
+    }
+    if (c.box > 0 && tot[3] > 0) {
+        e = launch_box(svs, pre + 3 * n1, tot[3], c, dbg, st);
         if (e != cudaSuccess) return e;
     }
     if ((e = mark(3)) != cudaSuccess) return e;

@@ -24,7 +24,7 @@ def _inputs(shape, seed, dtype="u8", n_tubes=3):
 
 def _oracle_params(orc, p):
     return orc.params(sigma=p.sigma, dt=p.dt, mu=p.mu, lambda1=p.lambda1, lambda2=p.lambda2, nu=p.nu, eps=p.eps,
-                      boundary=0 if p.boundary == "reference" else 1)
+                      sigma2=p.sigma2, boundary=0 if p.boundary == "reference" else 1)
 
 
 def _bits_equal(a, b):
@@ -82,6 +82,48 @@ def test_debug_fields_bit_exact(sigma, boundary, orc, ws_big, cuda):
     for i, n in enumerate(names):
         assert _bits_equal(got_fields[i], want_fields[i]), f"{n}: {_diff_report(got_fields[i], want_fields[i])}"
     assert _bits_equal(out.cpu().numpy(), want_out)
+
+
+BOX_CASES = [
+    # shape, sigma, sigma2, lambda1, lambda2, dtype, iters
+    ((20, 26, 30), 1.5, 1.0, 1.0, 1.0, "u8", 2),
+    ((24, 22, 28), 3.0, 2.5, 1.0, 0.5, "f32", 2),    # (int)sigma2 = 2, lambda1 != lambda2
+    ((9, 12, 10), 3.0, 1.0, 1.0, 1.0, "u8", 2),      # no valid blur region: f = 1 everywhere
+    ((30, 31, 33), 5.0, 1.0, 0.1, 0.1, "u8", 1),     # k = 35
+]
+
+
+@pytest.mark.parametrize("case", BOX_CASES, ids=lambda c: f"{c[0]}-s{c[1]}-box{c[2]}")
+def test_box_e_term_bit_exact(case, orc, ws_big, cuda):
+    """sigma2 >= 1: e = box sum of w (I_n - f(c))^2 (kernel.cu:25-55)."""
+    import torch
+    from rsf_gb300 import Params
+
+    shape, sigma, sigma2, l1, l2, dtype, iters = case
+    img, phi0, _ = _inputs(shape, seed=7, dtype=dtype)
+    p = Params(sigma=sigma, dt=0.1, mu=1.0, lambda1=l1, lambda2=l2, nu=65.025, eps=1.0, sigma2=sigma2)
+    tp = torch.from_numpy(phi0).to(cuda)
+    ws_big.evolve(torch.from_numpy(img).to(cuda), tp, p, iters)
+    ws_big.check()
+    got = tp.cpu().numpy()
+    want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), iters)
+    assert _bits_equal(got, want), _diff_report(got, want)
+    out, fields = ws_big.step_debug(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda), p)
+    want_out, want_fields = orc.step(phi0, img.astype(np.float32), _oracle_params(orc, p), debug=True)
+    got_fields = fields.cpu().numpy()
+    for i, n in enumerate(["f_out", "f_in", "e_out", "e_in"]):
+        assert _bits_equal(got_fields[i], want_fields[i]), f"{n}: {_diff_report(got_fields[i], want_fields[i])}"
+    assert _bits_equal(out.cpu().numpy(), want_out)
+
+
+def test_box_radius_limit(ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params, RsfError
+
+    img, phi0, _ = _inputs((12, 12, 12), seed=1)
+    with pytest.raises(RsfError):
+        ws_big.evolve(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda),
+                      Params(sigma=1.0, sigma2=9.0), 1)
 
 
 def test_batched_matches_plain(ws_big, cuda):

@@ -32,7 +32,7 @@ def _inputs(shape, seed):
     return img, phi0
 
 
-def _run_reference(rk, phi0, img, sigma, eps, iters, lam=1.0, mu=1.0, nu=65.025, dt=0.1):
+def _run_reference(rk, phi0, img, sigma, eps, iters, lam=1.0, mu=1.0, nu=65.025, dt=0.1, sigma2=0.0):
     import torch
 
     from oracle import ref_harness, rsf_oracle as orc
@@ -44,7 +44,8 @@ def _run_reference(rk, phi0, img, sigma, eps, iters, lam=1.0, mu=1.0, nu=65.025,
     phi = torch.from_numpy(phi0.ravel().copy()).to(dev)
     im = torch.from_numpy(img.astype(np.float32).ravel()).to(dev)
     taps = torch.from_numpy(orc.taps(sigma)).to(dev)
-    out, f = ref_harness.evolve(rk, phi, im, taps, W, H, L, iters, sigma=sigma, e=lam, dt=dt, v=nu, meu=mu)
+    out, f = ref_harness.evolve(rk, phi, im, taps, W, H, L, iters, sigma=sigma, e=lam, dt=dt, v=nu, meu=mu,
+                                sigma2=sigma2)
     return out.cpu().numpy().reshape(L, H, W), {k: v.cpu().numpy().reshape(L, H, W) for k, v in f.items()}
 
 
@@ -113,3 +114,25 @@ def test_portable_path_tracks_reference(rk, ws_big, cuda):
                   Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=0.2), 10)
     got = tp.cpu().numpy()
     assert float((np.sign(got) == np.sign(want)).mean()) >= 0.9999
+
+
+@pytest.mark.parametrize("sigma2", [1.0, 2.0])
+def test_box_e_term_reproduces_reference(rk, sigma2, ws_big, cuda):
+    """kernel.cu:25-55 with a box window: the oracle's e terms from the
+    reference's own fits equal the reference's, and the GPU in reference
+    arithmetic reproduces whole reference iterations bit for bit."""
+    import torch
+    from oracle import rsf_oracle as orc
+    from rsf_gb300 import Params
+
+    img, phi0 = _inputs((26, 28, 30), 14)
+    out, f = _run_reference(rk, phi0, img, 3.0, 0.2, 1, sigma2=sigma2)
+    eo, ei = orc.data_terms(img.astype(np.float32), f["fout"], f["fin"], int(sigma2))
+    assert _eq(eo, f["Eo"]) and _eq(ei, f["Ei"])
+    want, _ = _run_reference(rk, phi0, img, 3.0, 0.2, 3, sigma2=sigma2)
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=0.2, sigma2=sigma2,
+               arith="reference")
+    tp = torch.from_numpy(phi0).to(cuda)
+    ws_big.evolve(torch.from_numpy(img.astype(np.float32)).to(cuda), tp, p, 3)
+    got = tp.cpu().numpy()
+    assert _eq(got, want), f"{int((got != want).sum())} voxels differ"
