@@ -65,13 +65,19 @@ def segment(image, seed, params: Params, iters: int, cores=256, halo: int = 32, 
 
     image: uint8 or float32 (L, H, W) array or CUDA tensor; seed: same shape,
     inside where seed > threshold.  Tiles: `tiles` if given, else
-    plan(shape, cores, halo).  mode: "core" or "blend" stitching."""
+    plan(shape, cores, halo); cores="auto" lets the autotuner measure the
+    candidate core sizes first.  mode: "core" or "blend" stitching."""
     import torch
 
     device = torch.device(device)
     shape = tuple(int(s) for s in image.shape)
     if tuple(seed.shape) != shape:
         raise ValueError(f"image {shape} and seed {tuple(seed.shape)} differ in shape")
+    if tiles is None and cores == "auto":
+        from .autotune import tune_cores
+
+        dt = "u8" if str(image.dtype) in ("uint8", "torch.uint8") else "f32"
+        cores = tune_cores(shape, params, halo, dt, device=device).cores
     tiles = list(tiles) if tiles is not None else plan(shape, cores, halo)
     if max_chunk_voxels is None:
         free, _ = torch.cuda.mem_get_info(device)
@@ -110,7 +116,7 @@ def main(argv=None):
     ap.add_argument("--v", type=float, default=0.0001)
     ap.add_argument("--eps", type=float, default=0.2)
     ap.add_argument("--threshold", type=float, default=13.0)
-    ap.add_argument("--cores", type=int, default=256)
+    ap.add_argument("--cores", default="256", help="core size in voxels, or 'auto' to measure candidates")
     ap.add_argument("--halo", type=int, default=32)
     ap.add_argument("--mode", choices=("core", "blend"), default="core")
     args = ap.parse_args(argv)
@@ -121,7 +127,8 @@ def main(argv=None):
     while seed.ndim > 3 and seed.shape[0] == 1:
         seed = seed[0]
     p = Params.from_flags(sigma=args.sigma, dt=args.dt, meu=args.meu, e=args.e, v=args.v, eps=args.eps)
-    out = segment(image, seed, p, args.t, cores=args.cores, halo=args.halo, mode=args.mode,
+    cores = args.cores if args.cores == "auto" else int(args.cores)
+    out = segment(image, seed, p, args.t, cores=cores, halo=args.halo, mode=args.mode,
                   threshold=args.threshold)
     np.save(args.output, out.cpu().numpy())
     return 0

@@ -234,3 +234,19 @@ def test_grid_bounds_and_chunking():
     for g in groups:
         assert len(g) == 1 or sum(tiles[i].voxels for i in g) <= 20000
         assert g == list(range(g[0], g[-1] + 1))
+
+
+def test_autotuner_picks_the_fastest_owned_throughput():
+    from rsf_gb300 import Params, autotune
+
+    shape = (200, 300, 300)
+    plans = autotune.candidate_plans(shape, 32, (64, 128, 256, 512))
+    assert [c for c, _ in plans] == [64, 128, 256, 300]  # 512 clips to the largest extent
+    # a fake device: time proportional to evolved voxels plus a per-tile cost
+    res = autotune.tune_cores(shape, Params(sigma=3.0), 32, candidates=(64, 128, 256, 512),
+                              timer=lambda tiles: sum(t.voxels for t in tiles) / 3e10 + 2e-5 * len(tiles))
+    evolved = {c: sum(t.voxels for t in tiles) for c, tiles in plans}
+    assert res.cores == 300 and evolved[300] < evolved[64]
+    res2 = autotune.tune_cores(shape, Params(sigma=3.0), 32, candidates=(64, 128, 256, 512),
+                               timer=lambda tiles: 1e-3 + 0.0 * len(tiles) if len(tiles) > 4 else 1.0)
+    assert res2.cores in (64, 128)

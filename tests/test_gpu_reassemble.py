@@ -107,3 +107,14 @@ def test_driver_blend_mode_and_tensor_handoff(cuda, rsflib, orc):
     got_t = driver.segment(torch.from_numpy(img).cuda(), prob, p, 2, tiles=tiles, mode="blend",
                            threshold=0.5).cpu().numpy()
     assert np.array_equal(got_t.view(np.uint32), got.view(np.uint32))
+
+
+def test_autotuner_measures_candidates_on_device(cuda, rsflib):
+    from rsf_gb300 import Params, autotune, driver
+
+    p = Params(sigma=1.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=1.0)
+    res = autotune.tune_cores((48, 64, 64), p, halo=4, candidates=(16, 32, 64), iters=2)
+    assert res.cores in (16, 32, 64) and len(res.table) == 3 and all(r[1] > 0 for r in res.table)
+    img, seed_vol, _ = _driver_case((24, 30, 32))
+    out = driver.segment(img, seed_vol, p, 2, cores="auto", halo=4)
+    assert out.shape == img.shape and bool(torch.isfinite(out).all())
