@@ -668,6 +668,65 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
     S.DT[C1] = dn;  // plane rel+1
 }
 
+// x/y-interior step: the same arithmetic as stencil_step for blocks whose
+// threads and neighbour loads all lie inside the volume away from the x and
+// y faces (no x = 0, y = 0 or last-index rule applies, every thread is
+// inside).  The per-thread boundary selects and bounds tests drop out; the z
+// rules depend only on the plane, so they stay as block-uniform tests; phi is
+// read and written through pointers that advance one plane per step.
+template <int C, Arith A>
+__device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepConst &c, StencilState &S, int sc,
+                                                const float *&pp, float *&op, float (*Pb)[ST_WARPS][32],
+                                                float (*Gb)[2][ST_WARPS][32], unsigned *flag) {
+    constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
+    float p3 = 0.0f, exn = 0.0f, eyn = 0.0f;  // plane sc + 3
+    if (sc + 3 < k.L) {
+        p3 = __ldg(pp);
+        if (k.need_x) exn = __ldg(pp + k.xoff);
+        if (k.need_y) eyn = __ldg(pp + k.yoff);
+    }
+    const float dn = st_data(k, c, sc + 1);
+    pp += k.WH;
+    Pb[C2][k.w][k.lane] = S.P[C2];
+    const float p0 = S.P[C], p1 = S.P[C1], p2 = S.P[C2];
+    float L1 = __shfl_up_sync(0xffffffffu, p1, 1);
+    float R1 = __shfl_down_sync(0xffffffffu, p1, 1);
+    if (k.lane == 0) L1 = S.EX[C1];
+    if (k.lane == 31) R1 = S.EX[C1];
+    const float U1 = k.w > 0 ? Pb[C1][k.w - 1][k.lane] : S.EY[C1];
+    const float D1 = k.w < ST_WARPS - 1 ? Pb[C1][k.w + 1][k.lane] : S.EY[C1];
+    // gradient of plane pn = sc + 1 (z rules at the first and last plane; a
+    // plane outside the volume gets a value that no output reads)
+    const int pn = sc + 1;
+    const GN gn = gn_from<A>(L1, R1, U1, D1, pn > 0 ? p0 : p1, pn < k.L - 1 ? p2 : p1);
+    S.G[C1] = GN4{gn.nx, gn.gx, gn.nz, gn.gz};
+    Gb[C1][0][k.w][k.lane] = gn.ny;
+    Gb[C1][1][k.w][k.lane] = gn.gy;
+    __syncthreads();
+    const GN4 &gc = S.G[C];
+    const float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
+    const float gxL = __shfl_up_sync(0xffffffffu, gc.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gc.gx, 1);
+    if (sc >= k.z0 && k.outp) {
+        const float nyl = Gb[C][0][k.w - 1][k.lane], nyr = Gb[C][0][k.w + 1][k.lane];
+        const float gyl = Gb[C][1][k.w - 1][k.lane], gyr = Gb[C][1][k.w + 1][k.lane];
+        const GN4 &gp = S.G[C2];
+        const bool zlo = sc > 0, zhi = sc < k.L - 1;
+        const float nzl = zlo ? gp.nz : gc.nz, nzr = zhi ? gn.nz : gc.nz;
+        const float gzl = zlo ? gp.gz : gc.gz, gzr = zhi ? gn.gz : gc.gz;
+        const float kap = __fadd_rn(__fadd_rn(half_diff(nxR, nxL), half_diff(nyr, nyl)), half_diff(nzr, nzl));
+        const float lap = __fadd_rn(__fadd_rn(half_diff(gxR, gxL), half_diff(gyr, gyl)), half_diff(gzr, gzl));
+        const float dh = dirac<A>(p0, c.eps);
+        const float out = update_phi(p0, dh, S.DT[C], kap, lap, c.dt, c.nu, c.mu);
+        *op = out;
+        if (!isfinite(out)) atomicOr(flag, 1u);
+    }
+    op += k.WH;
+    S.P[C] = p3;
+    S.EX[C] = exn;
+    S.EY[C] = eyn;
+    S.DT[C1] = dn;
+}
+
 // ---------------------------------------------------------------------------
 // Box e-term, CUDA_RSF/kernel.cu:25-55 with s = (int)sigma2 >= 1: for every
 // voxel c, e = sum over the neighbours n of the (2s+1)^3 box that lie inside
@@ -809,6 +868,19 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     Pb[1][w][lane] = S.P[1];
     __syncthreads();
     const int count = k.z1 - k.first;
+    // x/y-interior blocks: every thread and neighbour load inside, no x or y
+    // face rule.
+    const bool interior = !DEBUG && x0 >= 2 && x0 + 32 <= k.W && y0 >= 2 && y0 + ST_OY + 2 <= k.H;
+    if (interior) {
+        const float *pp = k.phi + (ptrdiff_t)(k.first + 3) * (ptrdiff_t)k.WH;
+        float *op = k.phi_out + (ptrdiff_t)k.first * (ptrdiff_t)k.WH + (ptrdiff_t)k.col;
+        for (int i = 0; i < count; i += 3) {
+            stencil_step_in<0, A>(k, c, S, k.first + i, pp, op, Pb, Gb, flag);
+            if (i + 1 < count) stencil_step_in<1, A>(k, c, S, k.first + i + 1, pp, op, Pb, Gb, flag);
+            if (i + 2 < count) stencil_step_in<2, A>(k, c, S, k.first + i + 2, pp, op, Pb, Gb, flag);
+        }
+        return;
+    }
     for (int i = 0; i < count; i += 3) {
         stencil_step<0, A, DEBUG>(k, c, S, i, Pb, Gb, flag, dbg);
         if (i + 1 < count) stencil_step<1, A, DEBUG>(k, c, S, i + 1, Pb, Gb, flag, dbg);
