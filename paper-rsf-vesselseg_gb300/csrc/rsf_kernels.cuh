@@ -274,6 +274,92 @@ __device__ __forceinline__ void stream_axis(const Ring &rg, const StepConst &c, 
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// Ring with compile-time slots, for tap counts that are a multiple of the
+// ring depth RD (21 and 35 with RD = 7).  Blocks of K elements start at
+// multiples of K, so element base + j sits in slot j % RD, a constant of the
+// unrolled block; the global addresses advance by one stride per element
+// instead of being recomputed.  Same commit-group protocol as Ring: element
+// i is group i; iteration i refills the slot of element i-1 with element
+// i-1+RD and then waits until at most RD-1 groups are pending.
+template <int RD>
+__device__ __forceinline__ void cp_wait_depth() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(RD - 1) : "memory");
+}
+
+template <int RD>
+struct RingC {
+    float2 *base;              // this thread's slot 0; slot q at base + q * step
+    int step;
+    const float *next;         // global address of element `nfill`
+    size_t stride;
+    int nfill, n;
+    bool act;
+    // side stream: the aligned word around byte snext for elements >= sfirst
+    unsigned *sbase = nullptr;
+    const unsigned char *snext = nullptr;
+    size_t sstride = 0;
+    int sfirst = 0;
+    bool sact = false;
+    // `slot` is a constant after the caller's loop is unrolled
+    __device__ __forceinline__ void fill(int slot) {
+        if (act && nfill < n) {
+            cp_async8(base + slot * step, next);
+            if (sact && nfill >= sfirst)
+                cp_async4(sbase + slot * step,
+                          reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(snext) & ~(uintptr_t)3));
+        }
+        next += stride;  // addresses past the end are formed but never read
+        if (nfill >= sfirst) snext += sstride;
+        ++nfill;
+    }
+};
+
+template <int K, int RD, bool FIRST, bool GUARD, typename Emit>
+__device__ __forceinline__ void stream_block_c(RingC<RD> &rg, int base, const StepConst &c, float2 (&acc)[K],
+                                               Emit &emit) {
+    static_assert(K % RD == 0, "the ring depth must divide the tap count");
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        if (GUARD && base + j >= rg.n) break;
+        if (!(FIRST && j == 0)) {
+            rg.fill((j - 1 + RD) % RD);
+            cp_commit();
+        }
+        cp_wait_depth<RD>();
+        const float2 v = rg.base[(j % RD) * rg.step];
+#pragma unroll
+        for (int tt = 0; tt < K; ++tt) {
+            const int slot = (j - tt + K) % K;
+            if (tt == 0) acc[slot] = fma2(v, c.taps2[0], make_float2(0.f, 0.f));
+            else acc[slot] = fma2(v, c.taps2[tt], acc[slot]);
+        }
+        if (!FIRST || j >= K - 1) emit(base + j - (K - 1), acc[(j + 1) % K], j % RD);
+    }
+}
+
+template <int K, int RD, typename Emit>
+__device__ __forceinline__ void stream_axis_c(RingC<RD> &rg, const StepConst &c, Emit &emit) {
+#pragma unroll
+    for (int q = 0; q < RD; ++q) {
+        rg.fill(q);
+        cp_commit();
+    }
+    float2 acc[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] = make_float2(0.f, 0.f);
+    if (rg.n < K) {
+        stream_block_c<K, RD, true, true>(rg, 0, c, acc, emit);
+    } else {
+        stream_block_c<K, RD, true, false>(rg, 0, c, acc, emit);
+        int base = K;
+        for (; base + K <= rg.n; base += K) stream_block_c<K, RD, false, false>(rg, base, c, acc, emit);
+        if (base < rg.n) stream_block_c<K, RD, false, true>(rg, base, c, acc, emit);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+__host__ __device__ constexpr int ring_depth(int K) { return K % 7 == 0 ? 7 : RING; }
+
 // Register-blocked version for a tap count known only at run time: NB
 // consecutive outputs per call, same accumulation order.
 template <int NB>
@@ -313,6 +399,8 @@ __global__ void __launch_bounds__(YP_PAIRS) ypass_kernel(const SubVolDev *__rest
     const float *src = s.xb + f * ((size_t)s.Wp * s.H * s.L) + (size_t)z * s.H * s.Wp + x;
     float *dst = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)z * s.Hv * s.Wp + x;
     const size_t wp = (size_t)s.Wp;
+    // The y-pass is bound by HBM bandwidth: it keeps the deeper 8-slot ring
+    // (more loads in flight) rather than the compile-time-slot ring.
     auto emit = [&](int o, float2 v, int) { *reinterpret_cast<float2 *>(dst + (size_t)o * wp) = v; };
     const Ring rg = {ring + threadIdx.x, YP_PAIRS, src, wp, s.H, true};
     stream_axis<K>(rg, c, emit);
@@ -401,23 +489,48 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
     const size_t esz = c.img_f32 ? 4 : 1;
     const unsigned char *img0 = static_cast<const unsigned char *>(s.img) +
                                 (((size_t)(y + c.r)) * s.W + (size_t)(xc + c.r)) * esz;
-    Ring rg = {ring + threadIdx.x, ZP_PAIRS * 4, src, pstride, s.L, act};
-    rg.sbase = iring + threadIdx.x;
-    rg.side = img0;
-    rg.sstride = (size_t)s.W * s.H * esz;
-    rg.lag = c.r;
-    rg.first = 2 * c.r;
-    rg.sact = live;
-    auto emit = [&](int o, float2 v, int i) {
-        float I = 0.0f;
-        if (live) {
-            const unsigned wd = *rg.sslot(i);
-            if (c.img_f32) I = __uint_as_float(wd);
-            else I = (float)((wd >> (8 * (unsigned)(reinterpret_cast<uintptr_t>(rg.sbyte(i)) & 3))) & 0xffu);
-        }
-        fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
-    };
-    stream_axis<K>(rg, c, emit);
+    const size_t sstride = (size_t)s.W * s.H * esz;
+    if constexpr (K % ring_depth(K) == 0 && ring_depth(K) != RING) {
+        constexpr int RD = ring_depth(K);
+        RingC<RD> rg = {ring + threadIdx.x, ZP_PAIRS * 4, src, pstride, 0, s.L, act};
+        rg.sbase = iring + threadIdx.x;
+        rg.snext = img0 + (size_t)c.r * sstride;  // element 2r carries plane r, the first output's
+        rg.sstride = sstride;
+        rg.sfirst = 2 * c.r;
+        rg.sact = live;
+        // low two bits of the byte address of output o's image voxel:
+        // (shift0 + o * sstride) mod 4
+        const unsigned shift0 = (unsigned)(reinterpret_cast<uintptr_t>(img0 + (size_t)c.r * sstride) & 3);
+        const unsigned shift_step = (unsigned)(sstride & 3);
+        auto emit = [&](int o, float2 v, int slot) {
+            float I = 0.0f;
+            if (live) {
+                const unsigned wd = rg.sbase[slot * rg.step];
+                if (c.img_f32) I = __uint_as_float(wd);
+                else I = (float)((wd >> (8 * ((shift0 + (unsigned)o * shift_step) & 3u))) & 0xffu);
+            }
+            fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+        };
+        stream_axis_c<K, RD>(rg, c, emit);
+    } else {
+        Ring rg = {ring + threadIdx.x, ZP_PAIRS * 4, src, pstride, s.L, act};
+        rg.sbase = iring + threadIdx.x;
+        rg.side = img0;
+        rg.sstride = sstride;
+        rg.lag = c.r;
+        rg.first = 2 * c.r;
+        rg.sact = live;
+        auto emit = [&](int o, float2 v, int i) {
+            float I = 0.0f;
+            if (live) {
+                const unsigned wd = *rg.sslot(i);
+                if (c.img_f32) I = __uint_as_float(wd);
+                else I = (float)((wd >> (8 * (unsigned)(reinterpret_cast<uintptr_t>(rg.sbyte(i)) & 3))) & 0xffu);
+            }
+            fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+        };
+        stream_axis<K>(rg, c, emit);
+    }
 }
 
 template <bool DEBUG>
