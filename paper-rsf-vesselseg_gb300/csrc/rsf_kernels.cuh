@@ -139,16 +139,42 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
     const int x0 = tx * XT;
     const size_t row = ((size_t)z * s.H + y) * s.W;
     const float *phi = (parity ? s.phi[1] : s.phi[0]) + row;
-    for (int e = lane; e < span; e += 32) {
-        const int x = x0 + e;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (x < s.W) {
-            const float h = heaviside<A>(__ldg(phi + x), c.eps);
-            const float I = load_img(s.img, row + x, c.img_f32);
-            const float hi = __fsub_rn(1.0f, h);
-            v = make_float4(h, hi, __fmul_rn(I, h), __fmul_rn(I, hi));
+    if constexpr (K > 0) {
+        // all of the lane's loads first, so that they are in flight together
+        constexpr int NE = (XT + K - 1 + 31) / 32;
+        float ph[NE], im[NE];
+#pragma unroll
+        for (int q = 0; q < NE; ++q) {
+            const int e = lane + 32 * q, x = x0 + e;
+            const bool ok = e < span && x < s.W;
+            ph[q] = ok ? __ldg(phi + x) : 0.0f;
+            im[q] = ok ? load_img(s.img, row + x, c.img_f32) : 0.0f;
         }
-        in[e] = v;
+#pragma unroll
+        for (int q = 0; q < NE; ++q) {
+            const int e = lane + 32 * q;
+            if (e < span) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (x0 + e < s.W) {
+                    const float h = heaviside<A>(ph[q], c.eps);
+                    const float hi = __fsub_rn(1.0f, h);
+                    v = make_float4(h, hi, __fmul_rn(im[q], h), __fmul_rn(im[q], hi));
+                }
+                in[e] = v;
+            }
+        }
+    } else {
+        for (int e = lane; e < span; e += 32) {
+            const int x = x0 + e;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (x < s.W) {
+                const float h = heaviside<A>(__ldg(phi + x), c.eps);
+                const float I = load_img(s.img, row + x, c.img_f32);
+                const float hi = __fsub_rn(1.0f, h);
+                v = make_float4(h, hi, __fmul_rn(I, h), __fmul_rn(I, hi));
+            }
+            in[e] = v;
+        }
     }
     __syncwarp();
     // Pair 0 (H, 1-H) is staged in its own slab, pair 1 (I H, I (1-H)) in
