@@ -119,6 +119,12 @@ __device__ __forceinline__ float dT_axis(long long j, int q, int n, long long st
     return acc;
 }
 
+// delta(phi) with a fast division: the adjoint needs the derivative's value,
+// not the forward's bit pattern.
+__device__ __forceinline__ float dirac_fast(float phi, float eps) {
+    return __fdividef(0.318309886183790672f * eps, fmaf(phi, phi, eps * eps));
+}
+
 __global__ void adj_heaviside(AdjConst c, const float *phi, float *h, long long N) {
     for (long long i = grid_start(); i < N; i += grid_step()) h[i] = heaviside<Arith::Portable>(phi[i], c.eps);
 }
@@ -186,16 +192,17 @@ __global__ void adj_blur_z_data(AdjConst c, const float *in, const float *phi, c
         }
         const long long i = ((long long)(zv + c.r) * c.H + (yv + c.r)) * c.W + xv + c.r;
         const float I = img_at(img, i, c.img_f32);
-        const float fo = B[0] / B[1], fi = B[2] / B[3];
+        const float rb1 = __frcp_rn(B[1]), rb3 = __frcp_rn(B[3]);
+        const float fo = B[0] * rb1, fi = B[2] * rb3;
         const float dfo = I - fo, dfi = I - fi;
         eo_out[i] = dfo * dfo;
         ei_out[i] = dfi * dfi;
-        const float delta = dirac<Arith::Portable>(phi[i], c.eps);
+        const float delta = dirac_fast(phi[i], c.eps);
         const float data_bar = -u[i] * c.dt * delta;
         const float fo_bar = -2.0f * dfo * (c.l1 * data_bar);
         const float fi_bar = -2.0f * dfi * (-c.l2 * data_bar);
-        const float b1 = fo_bar / B[1], b2 = -fo_bar * fo / B[1];
-        const float b3 = fi_bar / B[3], b4 = -fi_bar * fi / B[3];
+        const float b1 = fo_bar * rb1, b2 = -fo_bar * fo * rb1;
+        const float b3 = fi_bar * rb3, b4 = -fi_bar * fi * rb3;
         pq[o] = b1 - b3;
         pq[n + o] = b2 - b4;
     }
@@ -262,10 +269,10 @@ __global__ void adj_normals(AdjConst c, const float *phi, float *nx, float *ny, 
         const int z = (int)(t1 / c.H);
         (void)x;
         const float gx = diff_x_at(c, phi, i), gy = diff_y_at(c, phi, i, y), gz = diff_z_at(c, phi, i, z);
-        const float s = sqrtf(gx * gx + gy * gy + gz * gz) + 1e-6f;
-        nx[i] = gx / s;
-        ny[i] = gy / s;
-        nz[i] = gz / s;
+        const float rs = __frcp_rn(sqrtf(gx * gx + gy * gy + gz * gz) + 1e-6f);
+        nx[i] = gx * rs;
+        ny[i] = gy * rs;
+        nz[i] = gz * rs;
     }
 }
 
@@ -277,7 +284,7 @@ __global__ void adj_stencil(AdjConst c, const float *phi, const void *img, const
     const long long N = (long long)c.W * c.H * c.L;
     const long long plane = (long long)c.W * c.H;
     double s_l1 = 0.0, s_l2 = 0.0, s_mu = 0.0, s_nu = 0.0;
-    auto kbar = [&](long long m) { return u[m] * c.dt * (c.nu * dirac<Arith::Portable>(phi[m], c.eps) - c.mu); };
+    auto kbar = [&](long long m) { return u[m] * c.dt * (c.nu * dirac_fast(phi[m], c.eps) - c.mu); };
     auto lbar = [&](long long m) { return u[m] * c.dt * c.mu; };
     for (long long i = grid_start(); i < N; i += grid_step()) {
         const int x = (int)(i % c.W);
@@ -286,16 +293,16 @@ __global__ void adj_stencil(AdjConst c, const float *phi, const void *img, const
         const int z = (int)(t1 / c.H);
         const float ph = phi[i], ui = u[i];
         const float I = img_at(img, i, c.img_f32);
-        const float delta = dirac<Arith::Portable>(ph, c.eps);
-        const float ddelta = -2.0f * ph * delta / (c.eps * c.eps + ph * ph);
+        const float delta = dirac_fast(ph, c.eps);
+        const float ddelta = __fdividef(-2.0f * ph * delta, fmaf(ph, ph, c.eps * c.eps));
         long long rx, lx, ry, ly, rz, lz;
         nb_x(c, i, x, rx, lx);
         nb_axis(i, y, c.H, c.W, ry, ly);
         nb_axis(i, z, c.L, plane, rz, lz);
         const float gx = 0.5f * (phi[rx] - phi[lx]), gy = 0.5f * (phi[ry] - phi[ly]), gz = 0.5f * (phi[rz] - phi[lz]);
         const float mag = sqrtf(gx * gx + gy * gy + gz * gz);
-        const float s = mag + 1e-6f;
-        const float inv_mag = mag > 0.0f ? 1.0f / mag : 0.0f;
+        const float rs = __frcp_rn(mag + 1e-6f);
+        const float inv_mag = mag > 0.0f ? __frcp_rn(mag) : 0.0f;
         const float kap = 0.5f * (nx[rx] - nx[lx]) + 0.5f * (ny[ry] - ny[ly]) + 0.5f * (nz[rz] - nz[lz]);
         const int yr = (int)((ry - i) / c.W) + y, yl = (int)((ly - i) / c.W) + y;
         const int zr = (int)((rz - i) / plane) + z, zl = (int)((lz - i) / plane) + z;
@@ -307,9 +314,9 @@ __global__ void adj_stencil(AdjConst c, const float *phi, const void *img, const
         const float lbx = dT_x(c, i, N, lbar), lby = dT_axis(i, y, c.H, c.W, lbar),
                     lbz = dT_axis(i, z, c.L, plane, lbar);
         const float ndot = nbx * nx[i] + nby * ny[i] + nbz * nz[i];
-        wx[i] = lbx + (nbx - ndot * gx * inv_mag) / s;
-        wy[i] = lby + (nby - ndot * gy * inv_mag) / s;
-        wz[i] = lbz + (nbz - ndot * gz * inv_mag) / s;
+        wx[i] = lbx + (nbx - ndot * gx * inv_mag) * rs;
+        wy[i] = lby + (nby - ndot * gy * inv_mag) * rs;
+        wz[i] = lbz + (nbz - ndot * gz * inv_mag) * rs;
         const bool valid = c.Wv > 0 && x >= c.r && x < c.r + c.Wv && y >= c.r && y < c.r + c.Hv && z >= c.r &&
                            z < c.r + c.Lv;
         float eo, ei;
