@@ -165,12 +165,34 @@ def cpu_sample(threads: int, budget_s: float = 15.0):
     one = max(time.perf_counter() - t0, 1e-3)
     iters = int(max(2, min(200, budget_s / one)))
     t0 = time.perf_counter()
-    orc.evolve(phi0, imgf, p, iters, threads)
+    want = orc.evolve(phi0, imgf, p, iters, threads)
     dt = time.perf_counter() - t0
     vox = img.size * iters
-    return {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+    base = {"value": vox / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"CPU oracle (C, OpenMP, {threads} threads), one {shape[2]}x{shape[1]}x{shape[0]} sub-volume "
                       f"of the workload's shape class, {iters} iterations, {dt:.1f} s"}
+    return base, (img, phi0, iters, want)
+
+
+def parity_on_sample(sample):
+    """The CUDA path on the CPU baseline's sample, against the oracle's result
+    for the same iterations: bit equality, sign (mask) agreement, max |dphi|."""
+    import numpy as np
+    import torch
+
+    from rsf_gb300 import Params, Workspace
+
+    img, phi0, iters, want = sample
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tp = torch.from_numpy(phi0).to(dev)
+    with Workspace(phi0.size) as ws:
+        ws.evolve(torch.from_numpy(img).to(dev), tp, Params(**PARAMS), iters)
+        ws.check()
+    got = tp.cpu().numpy()
+    return {"checked_against": "CPU oracle on the cpu_baseline sample",
+            "iterations": iters, "bit_identical": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32))),
+            "mask_agreement": float((np.sign(got) == np.sign(want)).mean()),
+            "max_abs_diff_over_max_abs_phi": float(np.abs(got.astype(np.float64) - want).max() / np.abs(want).max())}
 
 
 def run_reference(args):
@@ -207,6 +229,47 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def differentiable_sample(dev):
+    """The differentiable workload: 8 volumes of 128^3 (the 128^3 generator),
+    50 forward iterations with checkpoints every 10, soft-Dice loss against
+    the true mask, backward through the hand-written adjoint.  Returns the
+    forward + backward time per batch and the throughput in forward
+    voxel-iterations per second of the whole forward + backward job."""
+    import torch
+
+    from rsf_gb300 import Params, Workspace, autograd, synth
+
+    p = Params(sigma=3.0, dt=0.1, mu=0.2, lambda1=1.0, lambda2=1.0, nu=0.1, eps=1.0)
+    vols = []
+    for b in range(8):
+        spec = synth.VolumeSpec((128, 128, 128), 12, 2.0, 6.0, 40 + b)
+        img, phi0, mask = synth.make_volume_torch(spec, dev)
+        vols.append(((img.float() / 255.0).contiguous(), phi0, mask))
+    ws = Workspace(128 ** 3)
+
+    def batch():
+        for img, phi0, mask in vols:
+            x = phi0.clone().requires_grad_(True)
+            lam = torch.tensor(1.0, dtype=torch.float64, device=dev, requires_grad=True)
+            loss = autograd.soft_dice_loss(autograd.evolve(x, img, p, 50, lambda1=lam, checkpoint_every=10,
+                                                           workspace=ws), mask, p.eps)
+            loss.backward()
+
+    batch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    batch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ws.close()
+    return {"workload": "8 x 128^3, 50 iterations, checkpoints every 10, soft-Dice loss, gradients of phi0 and "
+                        "lambda1 (image scaled to [0, 1], mu 0.2, nu 0.1, eps 1, sigma 3)",
+            "fwd_bwd_ms_per_batch": ms, "value": 8 * 128 ** 3 * 50 / (ms / 1e3) / 1e9,
+            "unit": "forward Gvoxel-iter/s through forward + backward"}
 
 
 def run_ours(args):
@@ -276,6 +339,7 @@ def run_ours(args):
     value = vox_iters / (ms / 1e3) / 1e9
 
     # ---- plain per-volume path (one sub-volume at a time, no graph) ----
+    batched_out = [w.clone() for w in work]
     for w, p0 in zip(work, phi0s):
         w.copy_(p0)
     torch.cuda.synchronize()
@@ -286,6 +350,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
     plain_value = total_vox * ITERS / (plain_ms / 1e3) / 1e9
+    batched_equals_plain = all(torch.equal(a, b) for a, b in zip(batched_out, work))
+    del batched_out
 
     # ---- end to end: pinned host buffers -> evolve -> host ------------
     h_imgs = [im.cpu().pin_memory() for im in imgs]
@@ -349,14 +415,26 @@ def run_ours(args):
             "plain": {"value": plain_value, "unit": UNIT,
                       "how": "same sub-volumes evolved one at a time (rsf_evolve, no graph)"},
             "batched_vs_plain": value / world / plain_value,
+            "batched_equals_plain": batched_equals_plain,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "roofline": roofline,
             "kernels": kernels,
             "clocks": clk,
         }
+        # FP32 work of the separable 4-field schedule: 4 fields x 3 axes x k
+        # FMAs (2 flops each) plus ~120 pointwise flops per voxel-iteration,
+        # against the non-tensor FP32 rate of 152 SMs x 128 lanes x 2 flops at
+        # the SM clock seen during the timed region (a nominal figure).
+        f_alg = 24 * k + 120
+        fp32_peak = 152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
+        line["fp32"] = {"flops_per_voxel_iter": f_alg, "achieved_tflops": value * f_alg / 1e3,
+                        "nominal_peak_tflops": fp32_peak, "frac": value * f_alg / 1e3 / world / fp32_peak}
         if world == 1:
-            line["cpu_baseline"] = cpu_sample(os.cpu_count() or 1)
+            base, sample = cpu_sample(os.cpu_count() or 1)
+            line["cpu_baseline"] = base
+            line["parity"] = parity_on_sample(sample)
+            line["differentiable"] = differentiable_sample(dev)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
