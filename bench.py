@@ -148,6 +148,16 @@ def ncu_traffic_ratio(kernel: str):
     return None if k is None else float(k["ratio"])
 
 
+def ncu_warp_inst_per_voxel(kernel: str):
+    """Warp instructions issued per voxel by `kernel` in the committed ncu
+    capture (profiles/traffic.json), or None."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    k = json.loads(p.read_text()).get("kernels", {}).get(kernel)
+    return None if k is None or "warp_inst_per_voxel" not in k else float(k["warp_inst_per_voxel"])
+
+
 def cpu_sample(threads: int, budget_s: float = 15.0):
     """Times the CPU oracle on one sub-volume of the workload's shape class
     (the 64 x 288 x 288 corner tile), iterations sized to ~budget_s."""
@@ -402,6 +412,17 @@ def run_ours(args):
                 "step_alg_bytes_per_voxel_iter": sum(alg.values()) / total_vox,
                 "step_gbs": sum(alg.values()) * ITERS * args.steps / (ms / 1e3) / 1e9}
     launches = sum(v[1] for v in kt.values())
+    # The stencil, x-pass and z-pass are bound by instruction issue, not HBM:
+    # their issue-side roofline is warp instructions per second (the ncu
+    # count per voxel times this launch's voxels over its live time) against
+    # 152 SMs x 4 schedulers x one warp instruction per cycle at the SM clock.
+    ipv = ncu_warp_inst_per_voxel(dom)
+    if ipv is not None:
+        issue_peak = 152 * 4 * (clk.get("sm_mhz") or 2070.0) * 1e6
+        achieved = ipv * total_vox / (dk["ms_per_launch"] / 1e3)
+        roofline["issue"] = {"warp_inst_per_voxel": ipv, "achieved_warp_inst_per_s": achieved,
+                             "peak_warp_inst_per_s": issue_peak, "frac": achieved / issue_peak,
+                             "source": "ncu smsp__inst_executed.sum per voxel on the 320^3 case (profiles/traffic.json)"}
 
     if rank == 0:
         line = {
