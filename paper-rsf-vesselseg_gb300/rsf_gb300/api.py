@@ -121,6 +121,7 @@ class Workspace:
     def evolve(self, image, phi, params: Params, iters: int, stream=None):
         """Evolves torch CUDA tensor `phi` (float32, shape (L, H, W)) in place."""
         _require_cuda(image, phi)
+        _require_volume(phi, image)
         L, H, W = phi.shape
         check(self._lib.rsf_evolve(self.handle, ctypes.byref(params.to_c()), ctypes.c_void_p(image.data_ptr()),
                                    _dtype_code(image.dtype), ctypes.c_void_p(phi.data_ptr()), W, H, L, int(iters),
@@ -139,6 +140,7 @@ class Workspace:
         if out is None:
             out = torch.empty(seed.shape, dtype=torch.float32, device=seed.device)
         _require_cuda(out)
+        _require_volume(out, seed)
         L, H, W = seed.shape
         check(self._lib.rsf_signed_distance(self.handle, ctypes.c_void_p(seed.data_ptr()), _dtype_code(seed.dtype),
                                             ctypes.c_float(threshold), ctypes.c_void_p(out.data_ptr()), W, H, L,
@@ -151,10 +153,12 @@ class Workspace:
         lambda2, mu, nu) are added to it.  Returns `out` (new if None)."""
         import torch
         _require_cuda(image, phi, phi_bar)
+        _require_volume(phi, image, phi_bar)
         L, H, W = phi.shape
         if out is None:
             out = torch.empty_like(phi)
         _require_cuda(out)
+        _require_volume(out, phi)
         gp = None
         if param_grads is not None:
             _require_cuda(param_grads)
@@ -177,6 +181,7 @@ class Workspace:
         arr = (RsfSubvol * len(pairs))()
         for i, (img, phi) in enumerate(pairs):
             _require_cuda(img, phi)
+            _require_volume(phi, img)
             L, H, W = phi.shape
             arr[i] = RsfSubvol(phi.data_ptr(), img.data_ptr(), W, H, L)
         check(self._lib.rsf_evolve_batched(self.handle, ctypes.byref(params.to_c()), codes.pop(), arr, len(pairs),
@@ -187,6 +192,7 @@ class Workspace:
         """One iteration; returns (phi_out, fields[8]) as new CUDA tensors."""
         import torch
         _require_cuda(image, phi)
+        _require_volume(phi, image)
         L, H, W = phi.shape
         out = torch.empty_like(phi)
         fields = torch.empty((8, L, H, W), dtype=torch.float32, device=phi.device)
@@ -223,3 +229,18 @@ def _require_cuda(*ts):
             raise TypeError("expected CUDA tensors")
         if not t.is_contiguous():
             raise TypeError("expected contiguous tensors")
+
+
+def _require_volume(phi, *same_shape):
+    """phi: 3-D float32; every other tensor has phi's shape and device.  The C
+    ABI takes raw pointers and phi's extents, so a smaller image would be read
+    out of bounds: the shapes are checked here."""
+    import torch
+
+    if phi.dim() != 3 or phi.dtype != torch.float32:
+        raise TypeError(f"phi must be a 3-D float32 tensor (L, H, W), got {tuple(phi.shape)} {phi.dtype}")
+    for t in same_shape:
+        if tuple(t.shape) != tuple(phi.shape):
+            raise ValueError(f"shape {tuple(t.shape)} differs from phi's {tuple(phi.shape)}")
+        if t.device != phi.device:
+            raise ValueError("all tensors must be on phi's device")

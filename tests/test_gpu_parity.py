@@ -182,3 +182,22 @@ def test_reference_arith_close_to_portable(ws_big, cuda):
     a, b = outs
     assert float((np.sign(a) == np.sign(b)).mean()) >= 0.9999
     assert float(np.abs(a - b).max()) <= 1e-3 * float(np.abs(a).max())
+
+
+def test_python_api_rejects_mismatched_shapes(ws_big, cuda):
+    """The C ABI reads the image with phi's extents, so the Python face checks
+    the shapes before any launch."""
+    import torch
+    from rsf_gb300 import Params
+
+    p = Params(sigma=1.0)
+    phi = torch.zeros((10, 12, 14), device=cuda)
+    small = torch.zeros((10, 12, 13), dtype=torch.uint8, device=cuda)
+    with pytest.raises(ValueError):
+        ws_big.evolve(small, phi, p, 1)
+    with pytest.raises(ValueError):
+        ws_big.evolve_batched([(small, phi)], p, 1)
+    with pytest.raises(ValueError):
+        ws_big.step_adjoint(small, phi, phi.clone(), p)
+    with pytest.raises(TypeError):
+        ws_big.evolve(torch.zeros_like(phi, dtype=torch.uint8), phi.double(), p, 1)
