@@ -286,7 +286,7 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from rsf_gb300 import Params, Workspace, synth, tiling
+    from rsf_gb300 import Params, Workspace, copy_async, synth, tiling
     from rsf_gb300.dist import max_over_ranks
 
     world, rank, local = dist_env()
@@ -364,21 +364,40 @@ def run_ours(args):
     del batched_out
 
     # ---- end to end: pinned host buffers -> evolve -> host ------------
-    h_imgs = [im.cpu().pin_memory() for im in imgs]
-    h_phis = [p0.cpu().pin_memory() for p0 in phi0s]
-    h_out = [torch.empty_like(hp).pin_memory() for hp in h_phis]
-    d_imgs = [torch.empty_like(im) for im in imgs]
-    h2d = sum(x.numel() * x.element_size() for x in h_imgs) + sum(x.numel() * 4 for x in h_phis)
-    d2h = sum(x.numel() * 4 for x in h_phis)
+    # All tiles of a step live in one flat buffer per quantity (host and
+    # device), so each direction is one copy; the tiles are views into it.
+    # The copies run on the SMs (rsf_copy_async): on GB300 the copy engine's
+    # host-to-device rate drops to 53-69 GB/s once kernels have run, SM
+    # loads from pinned memory keep about 210 GB/s.
+    offs = [0]
+    for t in tiles:
+        offs.append(offs[-1] + t.voxels)
+    h_img = torch.empty(total_vox, dtype=torch.uint8, pin_memory=True)
+    h_phi = torch.empty(total_vox, dtype=torch.float32, pin_memory=True)
+    h_out = torch.empty(total_vox, dtype=torch.float32, pin_memory=True)
+    for i, (im, p0) in enumerate(zip(imgs, phi0s)):
+        h_img[offs[i]:offs[i + 1]].copy_(im.reshape(-1))
+        h_phi[offs[i]:offs[i + 1]].copy_(p0.reshape(-1))
+    h2d_bytes = h_img.numel() + 4 * h_phi.numel()
+    d2h_bytes = 4 * h_out.numel()
+
+    def device_set():
+        di = torch.empty(total_vox, dtype=torch.uint8, device=dev)
+        dp = torch.empty(total_vox, dtype=torch.float32, device=dev)
+        views = [(di[offs[i]:offs[i + 1]].view(t.shape), dp[offs[i]:offs[i + 1]].view(t.shape))
+                 for i, t in enumerate(tiles)]
+        return di, dp, views
+
+    del work, pairs, phi0s, imgs
+    torch.cuda.empty_cache()
+    sets = [device_set(), device_set()]
 
     def e2e_step():
-        for d, h in zip(d_imgs, h_imgs):
-            d.copy_(h, non_blocking=True)
-        for w, h in zip(work, h_phis):
-            w.copy_(h, non_blocking=True)
-        ws.evolve_batched(list(zip(d_imgs, work)), p, ITERS)
-        for o, w in zip(h_out, work):
-            o.copy_(w, non_blocking=True)
+        di, dp, views = sets[0]
+        copy_async(di, h_img)
+        copy_async(dp, h_phi)
+        ws.evolve_batched(views, p, ITERS)
+        copy_async(h_out, dp)
         torch.cuda.synchronize()
 
     e2e_step()
@@ -389,7 +408,48 @@ def run_ours(args):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
     e2e_s = max_over_ranks(e2e_s, dev)
-    e2e_value = total_vox * ITERS * world / e2e_s / 1e9
+    e2e_serial_value = total_vox * ITERS * world / e2e_s / 1e9
+
+    # Pipelined: step i+1's inputs go up and step i's level sets come down
+    # on a second stream while the evolution runs, through two sets of
+    # device buffers; every step's copies stay inside the timed region.
+    cs = torch.cuda.Stream(device=dev)
+    st = torch.cuda.current_stream(dev)
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+
+    def h2d(b):
+        copy_async(sets[b][0], h_img, stream=cs)
+        copy_async(sets[b][1], h_phi, stream=cs)
+        ev_in[b].record(cs)
+
+    def d2h(b):
+        cs.wait_event(ev_done[b])
+        copy_async(h_out, sets[b][1], stream=cs)
+
+    def pipeline(n):
+        h2d(0)
+        if n > 1:
+            h2d(1)
+        for i in range(n):
+            b = i % 2
+            st.wait_event(ev_in[b])
+            ws.evolve_batched(sets[b][2], p, ITERS, stream=st)
+            ev_done[b].record(st)
+            d2h(b)
+            if i + 2 < n:
+                h2d(b)  # after this set's download on the copy stream
+        torch.cuda.synchronize()
+
+    pipeline(2)
+    n_pipe = max(2, args.steps)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    pipeline(n_pipe)
+    pipe_s = (time.perf_counter() - t0) / n_pipe
+    pipe_s = max_over_ranks(pipe_s, dev)
+    e2e_value = total_vox * ITERS * world / pipe_s / 1e9
 
     # ---- roofline of the dominant kernel ------------------------------
     alg = algorithmic_bytes(tiles, k)
@@ -437,7 +497,12 @@ def run_ours(args):
                       "how": "same sub-volumes evolved one at a time (rsf_evolve, no graph)"},
             "batched_vs_plain": value / world / plain_value,
             "batched_equals_plain": batched_equals_plain,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
+                    "how": f"rsf_evolve_batched over {n_pipe} steps from pinned host buffers; each step's inputs "
+                           "copied up and results copied down on a second stream, overlapping the neighbouring "
+                           "steps' evolution (two device buffer sets)",
+                    "serial": {"value": e2e_serial_value,
+                               "how": "copy in, evolve, copy out, synchronise, one step at a time"}},
             "gpu_launches": int(launches),
             "roofline": roofline,
             "kernels": kernels,

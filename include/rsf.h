@@ -230,6 +230,16 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
                           const int64_t *core_x, const int64_t *core_y, const int64_t *core_z, int32_t mode,
                           float *out, int64_t W, int64_t H, int64_t L, void *stream);
 
+/* Copies `bytes` from src to dst with the device's SMs (16-byte loads and
+ * stores), asynchronously on `stream`.  Both addresses must be accessible
+ * from the device: device memory, or host memory that is pinned
+ * (cudaHostAlloc / cudaMallocHost) or registered (cudaHostRegister);
+ * RSF_ERR_INVALID_ARGUMENT otherwise (pageable host memory).  On GB300 it
+ * keeps about 210 GB/s between pinned host memory and the device where the
+ * copy engine's rate falls to 53-69 GB/s once kernels have run; the
+ * host-buffer entry points use it.  No counterpart in the reference. */
+rsf_status rsf_copy_async(void *dst, const void *src, size_t bytes, void *stream);
+
 /* Waits for the workspace's stream work and reports kernel-side errors
  * (non-finite phi when checking is enabled, CUDA launch errors). */
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream);

@@ -68,6 +68,27 @@ struct rsf_workspace {
     long long kernel_launches[rsf::NKERN] = {0, 0, 0, 0};
 };
 
+namespace {
+// True when the device can address `ptr` directly: device or managed memory,
+// or pinned / registered host memory (not pageable host memory).
+bool device_accessible(const void *ptr) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+}
+
+// Host <-> device staging copy: SM copy when the host side is pinned, else
+// the copy engine (pageable memory).
+cudaError_t stage_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+    const void *host = kind == cudaMemcpyHostToDevice ? src : dst;
+    if (device_accessible(host)) return rsf::launch_copy(dst, src, bytes, st);
+    return cudaMemcpyAsync(dst, src, bytes, kind, st);
+}
+}  // namespace
+
 extern "C" {
 
 int rsf_abi_version(void) { return RSF_ABI_VERSION; }
@@ -473,13 +494,13 @@ rsf_status rsf_evolve_host(rsf_workspace *ws, const rsf_params *p, const void *i
     }
     const size_t ib = nv * (dtype == RSF_F32 ? 4 : 1);
     cudaStream_t st = ws->capture_stream;
-    cudaError_t e = cudaMemcpyAsync(ws->stage_img, image_host, ib, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ws->stage_phi, phi_host, nv * sizeof(float), cudaMemcpyHostToDevice, st);
+    cudaError_t e = stage_copy(ws->stage_img, image_host, ib, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = stage_copy(ws->stage_phi, phi_host, nv * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "host to device");
     rsf_subvol sv = {ws->stage_phi, ws->stage_img, W, H, L};
     s = run(ws, p, dtype, &sv, 1, iters, st, false);
     if (s != RSF_OK) return s;
-    e = cudaMemcpyAsync(phi_host, ws->stage_phi, nv * sizeof(float), cudaMemcpyDeviceToHost, st);
+    e = stage_copy(phi_host, ws->stage_phi, nv * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "device to host");
     return RSF_OK;
@@ -619,6 +640,15 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
                                (int)W, (int)H, (int)L, st);
     if (e != cudaSuccess) return cuda_fail(e, "reassembly launch");
     return RSF_OK;
+}
+
+rsf_status rsf_copy_async(void *dst, const void *src, size_t bytes, void *stream) {
+    if (bytes == 0) return RSF_OK;
+    if (!dst || !src) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
+    if (!device_accessible(dst) || !device_accessible(src))
+        return fail(RSF_ERR_INVALID_ARGUMENT, "both addresses must be device memory or pinned / registered host memory");
+    cudaError_t e = rsf::launch_copy(dst, src, bytes, (cudaStream_t)stream);
+    return e == cudaSuccess ? RSF_OK : cuda_fail(e, "copy launch");
 }
 
 rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {

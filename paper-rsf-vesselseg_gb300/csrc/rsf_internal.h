@@ -121,6 +121,8 @@ struct TileDev {
 };
 cudaError_t launch_reassemble(const TileDev *d_tiles, const int n[3], const int *const cb[3], const int *const lo[3],
                               const int *const hi[3], int mode, float *out, int W, int H, int L, cudaStream_t st);
+// SM copy between device-accessible addresses (rsf_copy.cu).
+cudaError_t launch_copy(void *dst, const void *src, size_t bytes, cudaStream_t st);
 // Signed distance of {seed > thr}; scratch holds 3 * W*H*L words.
 cudaError_t launch_signed_distance(const void *seed, int f32, float thr, float *phi, int W, int H, int L,
                                    unsigned *scratch, cudaStream_t st);

@@ -4,6 +4,6 @@ The evolution runs in librsf_gb300.so (hand-written sm_103a CUDA behind the C
 ABI of include/rsf.h); this package is its Python face.
 """
 from ._lib import RsfError  # noqa: F401
-from .api import Params, Workspace, gaussian_taps  # noqa: F401
+from .api import Params, Workspace, copy_async, gaussian_taps  # noqa: F401
 
-__all__ = ["Params", "RsfError", "Workspace", "gaussian_taps"]
+__all__ = ["Params", "RsfError", "Workspace", "copy_async", "gaussian_taps"]

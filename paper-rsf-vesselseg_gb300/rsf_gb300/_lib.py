@@ -67,6 +67,7 @@ SIGNATURES = {
     "rsf_workspace_check": (ctypes.c_int, [_P, _P]),
     "rsf_signed_distance": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_float, _P, _I64, _I64, _I64, _P]),
     "rsf_reassemble": (ctypes.c_int, [_P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P, _I64, _I64, _I64, _P]),
+    "rsf_copy_async": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "rsf_step_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), _P, ctypes.c_int, _P, _P, _P, _P, _I64, _I64,
                                         _I64, _P]),
     "rsf_set_kernel_timing": (ctypes.c_int, [_P, ctypes.c_int]),

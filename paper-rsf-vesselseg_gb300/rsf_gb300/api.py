@@ -223,6 +223,21 @@ class Workspace:
                                         _dtype_code(image_dtype), ctypes.c_void_p(phi_ptr), W, H, L, int(iters)))
 
 
+def copy_async(dst, src, stream=None):
+    """dst <- src (torch tensors of equal byte size, each on the device or in
+    pinned host memory) with the device's SMs (rsf_copy_async): host <->
+    device transfers that keep their rate where the copy engine slows."""
+    nb = dst.numel() * dst.element_size()
+    if nb != src.numel() * src.element_size():
+        raise ValueError("dst and src differ in size")
+    if not (dst.is_contiguous() and src.is_contiguous()):
+        raise TypeError("expected contiguous tensors")
+    lib = _lib.load()
+    check(lib.rsf_copy_async(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr()), nb,
+                             ctypes.c_void_p(_stream_ptr(stream))))
+    return dst
+
+
 def _require_cuda(*ts):
     for t in ts:
         if not getattr(t, "is_cuda", False):

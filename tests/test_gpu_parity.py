@@ -201,3 +201,37 @@ def test_python_api_rejects_mismatched_shapes(ws_big, cuda):
         ws_big.step_adjoint(small, phi, phi.clone(), p)
     with pytest.raises(TypeError):
         ws_big.evolve(torch.zeros_like(phi, dtype=torch.uint8), phi.double(), p, 1)
+
+
+def test_copy_async_between_pinned_host_and_device(cuda, rsflib):
+    import torch
+    from rsf_gb300 import RsfError, copy_async
+
+    src = torch.randint(0, 256, (1 << 20,), dtype=torch.uint8).pin_memory()
+    dev = torch.empty(1 << 20, dtype=torch.uint8, device=cuda)
+    copy_async(dev, src)
+    back = torch.empty_like(src).pin_memory()
+    copy_async(back, dev)
+    torch.cuda.synchronize()
+    assert torch.equal(back, src)
+    # unaligned ranges and odd sizes take the byte path
+    d2 = torch.zeros(1000, dtype=torch.uint8, device=cuda)
+    copy_async(d2[3:1000], src[5:1002])
+    torch.cuda.synchronize()
+    assert torch.equal(d2[3:].cpu(), src[5:1002])
+    with pytest.raises(RsfError):
+        copy_async(dev, torch.empty(1 << 20, dtype=torch.uint8))  # pageable host memory
+
+
+def test_evolve_host_pinned_and_pageable_agree(orc, ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params
+
+    img, phi0, _ = _inputs((20, 24, 28), seed=9)
+    p = Params(sigma=1.5, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=1.0)
+    a = ws_big.evolve_host(img.copy(), phi0.copy(), p, 3)
+    ti = torch.from_numpy(img).pin_memory()
+    tp = torch.from_numpy(phi0.copy()).pin_memory()
+    ws_big.evolve_host_ptr(ti.data_ptr(), "uint8", tp.data_ptr(), phi0.shape, p, 3)
+    want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), 3)
+    assert _bits_equal(a, want) and _bits_equal(tp.numpy(), want)
