@@ -43,6 +43,17 @@ PARAMS = dict(sigma=SIGMA, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=0.001 * 
 WORKLOAD = ("config2: 48 uneven sub-volumes (extents 64-320 per axis, 256^3 cores + 32-voxel halos) cut from a "
             "512x1024x1024 synthetic vessel volume (800 tubes, radius U[1.5,8]); sigma 3 (21 taps), lambda 1, mu 1, "
             "nu 0.001*255^2, eps 1, dt 0.1; 150 iterations; phi float32, image uint8")
+SPEC = "CONFIG2"        # synth volume spec of the workload
+TILES = "config2_tiles"  # tiling of the workload
+
+# --workload gigavoxel: the 1024^3 volume in 27 tiles (384/384/256 cores +
+# 32-voxel halos, 1.53 G tile voxels), sigma 4, 200 iterations.  Not the
+# default line: a second measurement of the same kernels at larger scale.
+GIGAVOXEL = dict(
+    ITERS=200, SIGMA=4.0, SPEC="CONFIG3", TILES="config3_tiles",
+    WORKLOAD=("config3: 27 sub-volumes (384/384/256 cores + 32-voxel halos, extents 288-448) of a 1024^3 "
+              "synthetic vessel volume (2000 tubes, radius U[1,10]); sigma 4 (29 taps), lambda 1, mu 1, "
+              "nu 0.001*255^2, eps 1, dt 0.1; 200 iterations; phi float32, image uint8"))
 
 
 def dist_env():
@@ -296,10 +307,10 @@ def run_ours(args):
     dev = torch.device("cuda", local)
 
     # ---- inputs resident in HBM --------------------------------------
-    spec = synth.VolumeSpec(synth.CONFIG2.shape, synth.CONFIG2.n_tubes, synth.CONFIG2.r_min, synth.CONFIG2.r_max,
-                            synth.CONFIG2.seed + rank)
+    base = getattr(synth, SPEC)
+    spec = synth.VolumeSpec(base.shape, base.n_tubes, base.r_min, base.r_max, base.seed + rank)
     img_full, phi_full, _ = synth.make_volume_torch(spec, dev)
-    tiles = tiling.config2_tiles()
+    tiles = getattr(tiling, TILES)()
     imgs = [img_full[t.slices()].contiguous() for t in tiles]
     phi0s = [phi_full[t.slices()].contiguous() for t in tiles]
     del img_full, phi_full
@@ -490,8 +501,10 @@ def run_ours(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "subvolumes": len(tiles), "voxels": total_vox, "iterations": ITERS,
-                       "sigma": SIGMA, "taps": k, "step": "one 150-iteration evolution of all 48 sub-volumes",
-                       "l2": "inputs larger than L2 (phi 3.8 GB, y-pass fields 14 GB per iteration)",
+                       "sigma": SIGMA, "taps": k,
+                       "step": f"one {ITERS}-iteration evolution of all {len(tiles)} sub-volumes",
+                       "l2": f"inputs larger than L2 (phi {total_vox * 4 / 1e9:.1f} GB, y-pass fields "
+                             f"{total_vox * 16 / 1e9:.0f} GB per iteration)",
                        "parallelism": f"dp{world}"},
             "plain": {"value": plain_value, "unit": UNIT,
                       "how": "same sub-volumes evolved one at a time (rsf_evolve, no graph)"},
@@ -533,7 +546,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["config2", "gigavoxel"], default="config2",
+                    help="config2 (default, the 48-sub-volume batch) or gigavoxel (1024^3 in 27 tiles)")
     args = ap.parse_args()
+    if args.workload == "gigavoxel":
+        g = globals()
+        g.update(GIGAVOXEL)
+        g["PARAMS"] = dict(PARAMS, sigma=g["SIGMA"])
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
