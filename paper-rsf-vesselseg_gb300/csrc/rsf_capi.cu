@@ -5,7 +5,8 @@
 // cudaFree bracket, forward-declared at CUDA_RSF/main.cpp:56-71) and the
 // iteration loop of CUDA_RSF/main.cpp:222-314.  Here the state stays resident
 // in device memory, scratch lives in a caller-owned workspace, and a batch of
-// sub-volumes advances one iteration per three kernel launches.
+// sub-volumes advances one iteration per four kernel launches (x-pass, y-pass,
+// z-pass, stencil/update).
 #include <cuda_runtime.h>
 
 #include <algorithm>
