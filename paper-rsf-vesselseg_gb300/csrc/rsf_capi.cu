@@ -556,6 +556,8 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
     if (s != RSF_OK) return s;
     if ((s = check_shape(W, H, L)) != RSF_OK) return s;
     if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the box e-term (sigma2 >= 1) is not implemented");
+    // the stencil adjoint runs on 3-D grids: one z plane per grid row, 8 y per block
+    if (L > 65535 || H > 65535 * 8) return fail(RSF_ERR_SHAPE, "the adjoint supports L <= 65535 and H <= 524280");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
     if (!image || !phi || !phi_bar_in || !phi_bar_out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
     const int64_t n = W * H * L;
