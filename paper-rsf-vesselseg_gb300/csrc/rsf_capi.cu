@@ -50,10 +50,34 @@ struct rsf_workspace {
     SubVolDev *d_svs = nullptr;
     int *d_pre = nullptr;        // NKERN * (max_subvols + 1)
     unsigned *d_flag = nullptr;
-    SubVolDev *h_svs = nullptr;  // pinned staging of the table
-    int *h_pre = nullptr;
-    cudaEvent_t table_ev = nullptr;
-    bool table_pending = false;
+    // Pinned staging of the table, kStages slots used in turn: a call waits
+    // only for the upload of the call kStages before it, so consecutive
+    // calls do not make the host wait for the device.
+    static constexpr int kStages = 4;
+    SubVolDev *h_svs = nullptr;  // kStages * max_subvols
+    int *h_pre = nullptr;        // kStages * NKERN * (max_subvols + 1)
+    cudaEvent_t table_ev[kStages] = {};
+    bool table_pending[kStages] = {};
+    int stage = 0;
+    // Staging slot for the next upload; waits until its previous upload is done.
+    cudaError_t next_stage(SubVolDev **svs, int **pre) {
+        if (table_pending[stage]) {
+            cudaError_t e = cudaEventSynchronize(table_ev[stage]);
+            if (e != cudaSuccess) return e;
+            table_pending[stage] = false;
+        }
+        *svs = h_svs + (size_t)stage * max_subvols;
+        *pre = h_pre + (size_t)stage * rsf::NKERN * ((size_t)max_subvols + 1);
+        return cudaSuccess;
+    }
+    cudaError_t mark_stage(cudaStream_t st) {
+        cudaError_t e = cudaEventRecord(table_ev[stage], st);
+        if (e == cudaSuccess) {
+            table_pending[stage] = true;
+            stage = (stage + 1) % kStages;
+        }
+        return e;
+    }
     cudaStream_t capture_stream = nullptr;
     size_t bytes = 0;
     // host-buffer convenience path (allocated on first use)
@@ -164,7 +188,8 @@ static void ws_free(rsf_workspace *ws) {
     int cur = -1;
     cudaGetDevice(&cur);
     if (ws->device >= 0) cudaSetDevice(ws->device);
-    if (ws->table_ev) cudaEventSynchronize(ws->table_ev);
+    for (cudaEvent_t ev : ws->table_ev)
+        if (ev) cudaEventSynchronize(ev);
     cudaFree(ws->pool_phi2);
     cudaFree(ws->pool_x);
     cudaFree(ws->pool_y);
@@ -175,7 +200,8 @@ static void ws_free(rsf_workspace *ws) {
     cudaFree(ws->stage_phi);
     cudaFreeHost(ws->h_svs);
     cudaFreeHost(ws->h_pre);
-    if (ws->table_ev) cudaEventDestroy(ws->table_ev);
+    for (cudaEvent_t ev : ws->table_ev)
+        if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : ws->events) cudaEventDestroy(ev);
     if (ws->capture_stream) cudaStreamDestroy(ws->capture_stream);
     if (cur >= 0) cudaSetDevice(cur);
@@ -206,9 +232,12 @@ rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_wor
     alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
     alloc((void **)&ws->d_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
     alloc((void **)&ws->d_flag, 256);
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, (size_t)max_subvols * sizeof(SubVolDev));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws->table_ev, cudaEventDisableTiming);
+    const size_t ns = rsf_workspace::kStages;
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, ns * (size_t)max_subvols * sizeof(SubVolDev));
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&ws->h_pre, ns * rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
+    for (size_t i = 0; i < ns && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&ws->table_ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws->capture_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMemset(ws->d_flag, 0, 256);
     if (e == cudaSuccess) e = rsf::configure_device();
@@ -259,7 +288,8 @@ rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
 
 // Lays out a batch in the workspace pools and uploads the table.
 rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, rsf_dtype dtype,
-                   const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, cudaStream_t st) {
+                   const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, int *zc,
+                   cudaStream_t st) {
     if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
     if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
@@ -271,20 +301,25 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         total += svs[i].W * svs[i].H * svs[i].L;
     }
     if (total > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "batch larger than the workspace");
-    if (ws->table_pending) {
-        cudaError_t e = cudaEventSynchronize(ws->table_ev);
+    SubVolDev *h_svs = nullptr;
+    int *h_pre = nullptr;
+    {
+        cudaError_t e = ws->next_stage(&h_svs, &h_pre);
         if (e != cudaSuccess) return cuda_fail(e, "table event");
-        ws->table_pending = false;
     }
-    std::vector<int> wv(n);
+    std::vector<int> wv(n), whl(3 * (size_t)n);
     for (int i = 0; i < n; i++) {
         int Wv, Hv, Lv, Wp;
         rsf::valid_extents((int)svs[i].W, (int)svs[i].H, (int)svs[i].L, k, Wv, Hv, Lv, Wp);
         wv[i] = Wv;
+        whl[3 * i] = (int)svs[i].W;
+        whl[3 * i + 1] = (int)svs[i].H;
+        whl[3 * i + 2] = (int)svs[i].L;
     }
     *xb_w = rsf::choose_xb(wv.data(), n);
+    *zc = rsf::choose_zc(whl.data(), n);
     const int n1 = n + 1;
-    int *pre = ws->h_pre;
+    int *pre = h_pre;
     for (int j = 0; j < rsf::NKERN; j++) pre[j * n1] = 0;
     size_t off_v = 0, off_x = 0, off_y = 0;
     for (int i = 0; i < n; i++) {
@@ -295,7 +330,7 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         d.L = (int)svs[i].L;
         rsf::valid_extents(d.W, d.H, d.L, k, d.Wv, d.Hv, d.Lv, d.Wp);
         int tiles[rsf::NKERN];
-        rsf::tile_counts(d, kspec, *xb_w, tiles);
+        rsf::tile_counts(d, kspec, *xb_w, *zc, tiles);
         const size_t nv = (size_t)d.W * d.H * d.L;
         d.phi[0] = svs[i].phi;
         d.phi[1] = phi_out_override ? const_cast<float *>(phi_out_override[i]) : ws->pool_phi2 + off_v;
@@ -311,19 +346,18 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
             if (next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");
             pre[j * n1 + i + 1] = (int)next;
         }
-        ws->h_svs[i] = d;
+        h_svs[i] = d;
     }
     for (int j = 0; j < rsf::NKERN; j++) totals[j] = pre[j * n1 + n];
-    cudaError_t e = cudaMemcpyAsync(ws->d_svs, ws->h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaMemcpyAsync(ws->d_svs, h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ws->d_pre, ws->h_pre, rsf::NKERN * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaEventRecord(ws->table_ev, st);
+        e = cudaMemcpyAsync(ws->d_pre, h_pre, rsf::NKERN * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = ws->mark_stage(st);
     if (e != cudaSuccess) return cuda_fail(e, "table upload");
-    ws->table_pending = true;
     return RSF_OK;
 }
 
-StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n, int xb_w) {
+StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n, int xb_w, int zc) {
     StepConst c;
     std::memset(&c, 0, sizeof c);
     for (int i = 0; i < k; i++) {
@@ -343,6 +377,7 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
     c.xb_w = xb_w;
+    c.zc = zc;
     c.box = (int)p->sigma2;
     return c;
 }
@@ -403,11 +438,12 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     int k = 0;
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
-    int tot[rsf::NKERN], xb_w = 0;
-    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), dtype, nullptr, tot, &xb_w, st);
+    int tot[rsf::NKERN], xb_w = 0, zc = 0;
+    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), dtype, nullptr, tot, &xb_w, &zc,
+                st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
-    const StepConst c = make_const(p, k, taps, dtype, n, xb_w);
+    const StepConst c = make_const(p, k, taps, dtype, n, xb_w, zc);
     if (ws->timing) {
         s = timing_events(ws, iters, tot);
         if (s != RSF_OK) return s;
@@ -517,11 +553,11 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     if (s != RSF_OK) return s;
     rsf_subvol sv = {const_cast<float *>(phi), image, W, H, L};
     const float *outs[1] = {phi_out};
-    int tot[rsf::NKERN], xb_w = 0;
+    int tot[rsf::NKERN], xb_w = 0, zc = 0;
     cudaStream_t st = (cudaStream_t)stream;
-    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), dtype, outs, tot, &xb_w, st);
+    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), dtype, outs, tot, &xb_w, &zc, st);
     if (s != RSF_OK) return s;
-    const StepConst c = make_const(p, k, taps, dtype, 1, xb_w);
+    const StepConst c = make_const(p, k, taps, dtype, 1, xb_w, zc);
     const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};
     cudaError_t e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, 0, p->arith, ws->d_flag, &dbg, st);
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");
@@ -604,12 +640,13 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
         for (int j = 0; j <= n[a]; j++) cb[a][j] = (int)core[a][j];
         for (int j = 0; j < n[a]; j++) lo[a][j] = hi[a][j] = -1;
     }
-    if (ws->table_pending) {
-        cudaError_t e = cudaEventSynchronize(ws->table_ev);
+    SubVolDev *h_svs = nullptr;
+    int *h_pre = nullptr;
+    {
+        cudaError_t e = ws->next_stage(&h_svs, &h_pre);
         if (e != cudaSuccess) return cuda_fail(e, "table event");
-        ws->table_pending = false;
     }
-    rsf::TileDev *h = reinterpret_cast<rsf::TileDev *>(ws->h_svs);
+    rsf::TileDev *h = reinterpret_cast<rsf::TileDev *>(h_svs);
     for (int iz = 0; iz < nz; iz++)
         for (int iy = 0; iy < ny; iy++)
             for (int ix = 0; ix < nx; ix++) {
@@ -635,9 +672,8 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
             }
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(ws->d_svs, h, (size_t)ntiles * sizeof(rsf::TileDev), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaEventRecord(ws->table_ev, st);
+    if (e == cudaSuccess) e = ws->mark_stage(st);
     if (e != cudaSuccess) return cuda_fail(e, "tile table upload");
-    ws->table_pending = true;
     const int *pcb[3] = {cb[0], cb[1], cb[2]}, *plo[3] = {lo[0], lo[1], lo[2]}, *phi_[3] = {hi[0], hi[1], hi[2]};
     e = rsf::launch_reassemble(reinterpret_cast<const rsf::TileDev *>(ws->d_svs), n, pcb, plo, phi_, mode, out,
                                (int)W, (int)H, (int)L, st);

@@ -18,7 +18,7 @@ constexpr int ZB_ZB = 16;      // generic z-pass: outputs per thread along z
 constexpr int ST_OX = 30;      // stencil: output columns per warp (lanes 1..30)
 constexpr int ST_OY = 14;      // stencil: output rows per block (warps 1..14)
 constexpr int ST_WARPS = ST_OY + 2;
-constexpr int ST_ZC = 32;      // stencil: planes per block
+constexpr int ST_ZC = 64;      // stencil: planes per block (32 when that gives too few blocks)
 
 // The x-pass lane width (outputs per lane) is chosen per launch from these.
 constexpr int XB_CHOICES[2] = {5, 9};
@@ -54,6 +54,7 @@ struct StepConst {
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
     int xb_w;       // x-pass outputs per lane for this launch
+    int zc;         // stencil planes per block for this launch
     int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
 };
 
@@ -75,8 +76,9 @@ inline int kernel_k(int k, int arith, bool debug, int box = 0) {
 constexpr int MAX_BOX = 8;  // largest e-term box radius
 
 // Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
-void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]);
+void tile_counts(const SubVolDev &d, int kspec, int xb_w, int zc, int tiles[NKERN]);
 int choose_xb(const int *Wv, int n);
+int choose_zc(const int *whl, int n);  // whl: W, H, L of each sub-volume
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
 
 // One iteration.  With `ev` (NKERN + 1 events) the events are recorded before

@@ -891,7 +891,7 @@ __global__ void __launch_bounds__(ST_WARPS * 32) box_kernel(const SubVolDev *__r
     const int tz = t / nty;
     const int x = tx * ST_OX - 1 + lane, y = ty * ST_OY - 1 + w;
     if (lane < 1 || lane > ST_OX || w < 1 || w > ST_OY || x >= s.W || y >= s.H) return;
-    const int z0 = tz * ST_ZC, z1 = min(z0 + ST_ZC, s.L);
+    const int z0 = tz * c.zc, z1 = min(z0 + c.zc, s.L);
     const int bs = c.box, r = c.r;
     const double wt = 1.0 / (double)((2 * bs + 1) * (2 * bs + 1));
     const size_t WH = (size_t)s.W * s.H, nvalid = (size_t)s.Wp * s.Hv * s.Lv;
@@ -958,8 +958,8 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     k.y = y0 - 1 + w;
     k.w = w;
     k.lane = lane;
-    k.z0 = tz * ST_ZC;
-    k.z1 = min(k.z0 + ST_ZC, k.L);
+    k.z0 = tz * c.zc;
+    k.z1 = min(k.z0 + c.zc, k.L);
     k.first = k.z0 - 2;
     k.in = k.x >= 0 && k.x < k.W && k.y >= 0 && k.y < k.H;
     k.outp = k.in && lane >= 1 && lane <= ST_OX && w >= 1 && w <= ST_OY;

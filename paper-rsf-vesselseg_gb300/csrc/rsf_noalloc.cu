@@ -119,9 +119,11 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     d.db = xfields;
     d.yb = yfields;
     const int xb_w = rsf::choose_xb(&d.Wv, 1);
+    const int whl[3] = {d.W, d.H, d.L};
+    const int zc = rsf::choose_zc(whl, 1);
     const int kspec = rsf::kernel_k(k, p->arith, false);
     int tiles[rsf::NKERN];
-    rsf::tile_counts(d, kspec, xb_w, tiles);
+    rsf::tile_counts(d, kspec, xb_w, zc, tiles);
     int pre[2 * rsf::NKERN];  // per kernel: {0, tiles}
     for (int j = 0; j < rsf::NKERN; j++) {
         pre[2 * j] = 0;
@@ -147,6 +149,7 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     c.img_f32 = dtype == RSF_F32;
     c.nsv = 1;
     c.xb_w = xb_w;
+    c.zc = zc;
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // The table copies come from pageable host memory: they return once the

@@ -30,7 +30,17 @@ int choose_xb(const int *Wv, int n) {
     return best;
 }
 
-void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]) {
+// Stencil planes per block: ST_ZC, or half of it when the batch would then
+// give fewer than four waves of blocks (two resident per SM on 152 SMs).
+int choose_zc(const int *whl, int n) {
+    long long blocks = 0;
+    for (int i = 0; i < n; i++)
+        blocks += (long long)((whl[3 * i] + ST_OX - 1) / ST_OX) * ((whl[3 * i + 1] + ST_OY - 1) / ST_OY) *
+                  ((whl[3 * i + 2] + ST_ZC - 1) / ST_ZC);
+    return blocks >= 4LL * 2 * 152 ? ST_ZC : ST_ZC / 2;
+}
+
+void tile_counts(const SubVolDev &d, int kspec, int xb_w, int zc, int tiles[NKERN]) {
     const bool valid = d.Wv > 0;
     const int xt = 32 * xb_w;
     tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L : 0;
@@ -40,7 +50,7 @@ void tile_counts(const SubVolDev &d, int kspec, int xb_w, int tiles[NKERN]) {
     if (!valid) tiles[2] = 0;
     else if (kspec == 0) tiles[2] = ((d.Wv + ZB_TX - 1) / ZB_TX) * ((d.Lv + ZB_ZB - 1) / ZB_ZB) * d.Hv;
     else tiles[2] = ((d.Wv + 2 * ZP_PAIRS - 1) / (2 * ZP_PAIRS)) * d.Hv;
-    tiles[3] = ((d.W + ST_OX - 1) / ST_OX) * ((d.H + ST_OY - 1) / ST_OY) * ((d.L + ST_ZC - 1) / ST_ZC);
+    tiles[3] = ((d.W + ST_OX - 1) / ST_OX) * ((d.H + ST_OY - 1) / ST_OY) * ((d.L + zc - 1) / zc);
 }
 
 // Raises the dynamic shared-memory limit of the x-pass instantiations on the
