@@ -8,7 +8,7 @@ namespace rsf {
 constexpr int MAXK = 128;  // largest supported tap count (sigma up to ~18)
 
 // Kernel tilings (the launchers derive tile counts from them).
-constexpr int XP_ROWS = 8;     // x-pass: rows per block (one warp per row)
+constexpr int XP_ROWS = 4;     // x-pass: rows per block (one warp per row)
 constexpr int YP_PAIRS = 128;  // y-pass: column pairs per block (one thread each)
 constexpr int YB_TX = 128;     // generic y-pass: columns per block
 constexpr int YB_YB = 16;      // generic y-pass: outputs per thread along y
