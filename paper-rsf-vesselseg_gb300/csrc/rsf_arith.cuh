@@ -1,7 +1,7 @@
 // rsf_arith.cuh -- pointwise arithmetic of the RSF step on the device.
 //
 // Every operation is an explicit correctly-rounded intrinsic (__fmaf_rn,
-// __fmul_rn, __fadd_rn, __fsub_rn, __fdiv_rn, __fsqrt_rn), so nvcc can neither
+// __fmul_rn, __fadd_rn, __fsub_rn, __fdiv_rn, __frcp_rn, __fsqrt_rn), so nvcc can neither
 // contract nor reorder anything.  The portable definitions (Arith::Portable)
 // are the exact same operation sequences as the CPU oracle's, which makes the
 // GPU result bit-identical to the oracle on every input.  Arith::Reference
@@ -22,7 +22,7 @@ enum class Arith : int { Portable = 0, Reference = 1 };
 __device__ __forceinline__ float atan_portable(float x) {
     const float a = fabsf(x);
     const bool big = a > 1.0f;
-    const float u = big ? __fdiv_rn(1.0f, a) : a;
+    const float u = big ? __frcp_rn(a) : a;  // the correctly rounded 1/a, as 1.0f / a
     const float z = __fmul_rn(u, u);
     float r = -0x1.d727360000000p-10f;
     r = __fmaf_rn(r, z, 0x1.6636cc0000000p-7f);
