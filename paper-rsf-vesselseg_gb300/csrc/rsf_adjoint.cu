@@ -24,11 +24,13 @@
 // among its three axis neighbours whose right index is j, and -0.5 v(m) for
 // every m whose left index is j, so boundary rules transpose exactly.
 //
-// Kernels (one thread per voxel, grid-stride): blur recompute x, y, z (the z
-// kernel also forms the data-term adjoint), transposed blur z, y, x (the x
-// kernel forms H_bar), gradients and unit normals, the pointwise terms with
-// the parameter sums, the stencil adjoint, and the final D^T gather.  Scratch comes from the
-// workspace pools; the layout is given in launch_step_adjoint.
+// Kernels: H; blur recompute x, y, z (the z kernel also forms the data-term
+// adjoint); transposed blur z, y, x (the x kernel forms H_bar); gradients and
+// unit normals; the pointwise terms with the parameter sums; the stencil
+// adjoint w; the final D^T gather.  The blurs along y and z compute several
+// consecutive outputs per thread; the last three kernels run on 3-D grids,
+// the others are grid-stride loops.  Scratch comes from the workspace pools;
+// the layout is given in launch_step_adjoint.
 #include <cuda_runtime.h>
 
 #include "rsf_arith.cuh"
