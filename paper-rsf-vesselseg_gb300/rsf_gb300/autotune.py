@@ -61,6 +61,17 @@ def pick(shape: Sequence[int], measurements: Sequence[Tuple[int, Sequence[Tile],
     return TuneResult(best[0], best[1], table)
 
 
+def smooth_phi(shape: Sequence[int], device="cpu"):
+    """A smooth level set in [-3, 3], float32 (L, H, W): a product of sines
+    whose sign changes every 8 to 14 voxels along each axis.  The timing runs
+    evolve it rather than noise, so that they stay finite for any parameters."""
+    import torch
+
+    z, y, x = (torch.arange(int(n), device=device, dtype=torch.float32) for n in shape)
+    return (3.0 * torch.sin(0.37 * x)[None, None, :] * torch.sin(0.29 * y + 1.0)[None, :, None]
+            * torch.sin(0.23 * z + 2.0)[:, None, None]).contiguous()
+
+
 def _time_plan(tiles: Sequence[Tile], params: Params, dtype, iters: int, device) -> float:
     import torch
 
@@ -72,8 +83,7 @@ def _time_plan(tiles: Sequence[Tile], params: Params, dtype, iters: int, device)
         for t in tiles:
             img = (torch.randint(0, 256, t.shape, generator=gen, device=device, dtype=torch.uint8)
                    if dtype == "u8" else torch.rand(t.shape, generator=gen, device=device))
-            phi = torch.randn(t.shape, generator=gen, device=device).mul_(3.0).contiguous()
-            pairs.append((img, phi))
+            pairs.append((img, smooth_phi(t.shape, device)))
         ws.evolve_batched(pairs, params, 1)  # warm-up (graph capture, table upload)
         torch.cuda.synchronize(device)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -250,3 +250,18 @@ def test_autotuner_picks_the_fastest_owned_throughput():
     res2 = autotune.tune_cores(shape, Params(sigma=3.0), 32, candidates=(64, 128, 256, 512),
                                timer=lambda tiles: 1e-3 + 0.0 * len(tiles) if len(tiles) > 4 else 1.0)
     assert res2.cores in (64, 128)
+
+
+def test_autotuner_level_set_is_smooth_and_bounded():
+    import torch
+    from rsf_gb300 import autotune
+
+    phi = autotune.smooth_phi((20, 30, 40))
+    assert phi.shape == (20, 30, 40) and phi.dtype == torch.float32 and phi.is_contiguous()
+    assert float(phi.abs().max()) <= 3.0 and float(phi.min()) < 0.0 < float(phi.max())
+    # neighbouring voxels differ by at most the field's Lipschitz bound
+    steps = [phi.diff(dim=d).abs().max() for d in range(3)]
+    assert max(float(s) for s in steps) <= 3.0 * 0.37 + 1e-6
+    z, y, x = 5, 7, 11
+    want = 3.0 * np.sin(0.37 * x) * np.sin(0.29 * y + 1.0) * np.sin(0.23 * z + 2.0)
+    assert abs(float(phi[z, y, x]) - want) < 1e-5
