@@ -4,6 +4,7 @@
 #include "npy_io.h"
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -63,6 +64,7 @@ std::string npy_load(const std::string &path, NpyVolume &out) {
     } else {
         return path + ": unsupported .npy version";
     }
+    if (hlen > (1u << 20)) return path + ": header too long";
     std::string hdr(hlen, '\0');
     if (!f.read(&hdr[0], hlen)) return path + ": truncated header";
     const std::string descr = dict_value(hdr, "descr");
@@ -77,13 +79,19 @@ std::string npy_load(const std::string &path, NpyVolume &out) {
         while (std::getline(ss, tok, ',')) {
             size_t a = tok.find_first_not_of(' ');
             if (a == std::string::npos) continue;
-            dims.push_back(std::stoll(tok.substr(a)));
+            char *end = nullptr;
+            const long long d = std::strtoll(tok.c_str() + a, &end, 10);
+            while (end && *end == ' ') ++end;
+            if (!end || end == tok.c_str() + a || (*end != '\0' && *end != 'L')) return path + ": malformed shape";
+            dims.push_back((int64_t)d);
         }
     }
     while (dims.size() > 3 && dims.front() == 1) dims.erase(dims.begin());
     if (dims.size() != 3) return path + ": expected a 3-D array";
     for (int64_t d : dims)
         if (d < 1) return path + ": empty array";
+        else if (d > (int64_t(1) << 31)) return path + ": extent too large";
+    if (dims[0] * dims[1] > (int64_t(1) << 40) / dims[2]) return path + ": array too large";
     const size_t n = (size_t)(dims[0] * dims[1] * dims[2]);
     const bool fortran_order = fortran.find("True") != std::string::npos;
     const char endian = descr[0];

@@ -123,3 +123,28 @@ def test_cli_npy_reader_rejects_bad_files_and_shape_mismatch(tmp_path):
     np.save(seed, np.zeros((4, 5, 6), dtype=np.complex64))
     r = _run("--image", str(img), "--binary", str(seed))
     assert r.returncode == 3 and "unsupported dtype" in r.stderr
+
+
+def _raw_npy(header: str, version=1, data=b""):
+    hdr = header.encode("latin1")
+    if version == 1:
+        return b"\x93NUMPY\x01\x00" + len(hdr).to_bytes(2, "little") + hdr + data
+    return b"\x93NUMPY" + bytes([version, 0]) + len(hdr).to_bytes(4, "little") + hdr + data
+
+
+@pytest.mark.parametrize("raw,msg", [
+    (_raw_npy("{'descr': '<f4', 'fortran_order': False, 'shape': (4, x5, 6), }\n"), "malformed shape"),
+    (_raw_npy("{'descr': '<f4', 'fortran_order': False, 'shape': (3000000000, 4, 4), }\n"), "extent too large"),
+    (_raw_npy("{'descr': '<f4', 'fortran_order': False, 'shape': (2147483648, 2147483648, 2), }\n"),
+     "array too large"),
+    (b"\x93NUMPY\x02\x00" + (1 << 21).to_bytes(4, "little"), "header too long"),
+    (_raw_npy("{'descr': '<f4', 'fortran_order': False, 'shape': (2, 2, 2), }\n", data=b"\0" * 12),
+     "truncated data"),
+])
+def test_cli_npy_reader_rejects_malformed_headers(tmp_path, raw, msg):
+    img = tmp_path / "img.npy"
+    np.save(img, np.zeros((2, 2, 2), dtype=np.uint8))
+    bad = tmp_path / "bad.npy"
+    bad.write_bytes(raw)
+    r = _run("--image", str(img), "--binary", str(bad))
+    assert r.returncode == 3 and msg in r.stderr, r.stderr
