@@ -1,11 +1,13 @@
 """A small, self-contained evolution for profiler captures.
 
     python paper-rsf-vesselseg_gb300/rsf_gb300/profile_case.py --n 320 --sigma 3 --iters 2
+    python paper-rsf-vesselseg_gb300/rsf_gb300/profile_case.py --n 128 --sigma 3 --iters 1 --adjoint 2
 
 Evolves one n^3 volume (a smooth level set and a random uint8 image, made on
 the device) for `iters` iterations through the C ABI and exits.  At n = 320
 the working set is about 1.4 GB, larger than L2, so DRAM counters of one
-launch mean what they say.
+launch mean what they say.  `--adjoint S` then runs S adjoint steps
+(rsf_step_adjoint, eleven launches each) at the evolved level set.
 """
 from __future__ import annotations
 
@@ -21,6 +23,7 @@ def main():
     ap.add_argument("--n", type=int, default=320)
     ap.add_argument("--sigma", type=float, default=3.0)
     ap.add_argument("--iters", type=int, default=2)
+    ap.add_argument("--adjoint", type=int, default=0, help="adjoint steps after the evolution")
     args = ap.parse_args()
     import torch
 
@@ -39,8 +42,15 @@ def main():
     with Workspace(n ** 3) as ws:
         ws.evolve(img, phi, p, args.iters)
         ws.check()
+        if args.adjoint:
+            u = torch.randn(phi.shape, device=dev, generator=gen)
+            out = torch.empty_like(phi)
+            grads = torch.zeros(4, dtype=torch.float64, device=dev)
+            for _ in range(args.adjoint):
+                ws.step_adjoint(img, phi, u, p, out=out, param_grads=grads)
+            ws.check()
     torch.cuda.synchronize()
-    print(f"profile case done: {n}^3, sigma {args.sigma}, {args.iters} iterations")
+    print(f"profile case done: {n}^3, sigma {args.sigma}, {args.iters} iterations, {args.adjoint} adjoint steps")
 
 
 if __name__ == "__main__":
