@@ -265,3 +265,46 @@ def test_autotuner_level_set_is_smooth_and_bounded():
     z, y, x = 5, 7, 11
     want = 3.0 * np.sin(0.37 * x) * np.sin(0.29 * y + 1.0) * np.sin(0.23 * z + 2.0)
     assert abs(float(phi[z, y, x]) - want) < 1e-5
+
+
+def test_plan_properties_over_random_grids():
+    """For random shapes, core sizes (int or explicit bounds) and halos: the
+    cores partition the volume, every tile is its core grown by the halo and
+    clipped at the faces, grid_bounds recovers the bounds, and cut followed
+    by core reassembly is the identity."""
+    from oracle import reassembly
+    from rsf_gb300 import tiling
+
+    rng = np.random.default_rng(123)
+    for _ in range(40):
+        shape = tuple(int(v) for v in rng.integers(1, 40, size=3))
+        cores = []
+        for n in shape:
+            if rng.random() < 0.5:
+                cores.append(int(rng.integers(1, n + 3)))
+            else:
+                cuts = sorted(set(int(v) for v in rng.integers(1, max(n, 2), size=int(rng.integers(0, 4)))))
+                cores.append([0] + [c for c in cuts if 0 < c < n] + [n])
+        halo = int(rng.integers(0, 6))
+        tiles = tiling.plan(shape, tuple(cores), halo)
+        owner = np.zeros(shape, dtype=np.int32)
+        for t in tiles:
+            owner[t.core_slices()] += 1
+            for a in range(3):
+                assert t.lo[a] == max(0, t.clo[a] - halo) and t.hi[a] == min(shape[a], t.chi[a] + halo)
+                assert 0 <= t.lo[a] <= t.clo[a] < t.chi[a] <= t.hi[a] <= shape[a]
+        assert np.all(owner == 1)
+        bounds = tiling.grid_bounds(tiles)
+        for a, n in enumerate(shape):
+            want = list(range(0, n, cores[a])) + [n] if isinstance(cores[a], int) else cores[a]
+            assert bounds[a] == want
+        vol = rng.normal(size=shape).astype(np.float32)
+        assert np.array_equal(reassembly.reassemble_cores(shape, tiles, tiling.cut(vol, tiles)), vol)
+
+
+def test_plan_rejects_bounds_that_do_not_partition():
+    from rsf_gb300 import tiling
+
+    for bad in ([0, 5, 5, 10], [1, 10], [0, 12], [0, 7, 3, 10]):
+        with pytest.raises(ValueError):
+            tiling.plan((10, 10, 10), (bad, 5, 5), 2)
