@@ -94,22 +94,26 @@ struct rsf_workspace {
 };
 
 namespace {
-// True when the device can address `ptr` directly: device or managed memory,
-// or pinned / registered host memory (not pageable host memory).
-bool device_accessible(const void *ptr) {
+// The address through which the device reads or writes `ptr`: the pointer
+// itself for device or managed memory, the mapped address for pinned or
+// registered host memory, null for pageable host memory.
+void *device_view(const void *ptr) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return nullptr;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged)
+        return a.devicePointer;
+    return nullptr;
 }
 
 // Host <-> device staging copy: SM copy when the host side is pinned, else
 // the copy engine (pageable memory).
 cudaError_t stage_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
-    const void *host = kind == cudaMemcpyHostToDevice ? src : dst;
-    if (device_accessible(host)) return rsf::launch_copy(dst, src, bytes, st);
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    void *hv = device_view(h2d ? src : dst);
+    if (hv) return h2d ? rsf::launch_copy(dst, hv, bytes, st) : rsf::launch_copy(hv, src, bytes, st);
     return cudaMemcpyAsync(dst, src, bytes, kind, st);
 }
 }  // namespace
@@ -684,9 +688,10 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
 rsf_status rsf_copy_async(void *dst, const void *src, size_t bytes, void *stream) {
     if (bytes == 0) return RSF_OK;
     if (!dst || !src) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
-    if (!device_accessible(dst) || !device_accessible(src))
+    void *dv = device_view(dst), *sv = device_view(src);
+    if (!dv || !sv)
         return fail(RSF_ERR_INVALID_ARGUMENT, "both addresses must be device memory or pinned / registered host memory");
-    cudaError_t e = rsf::launch_copy(dst, src, bytes, (cudaStream_t)stream);
+    cudaError_t e = rsf::launch_copy(dv, sv, bytes, (cudaStream_t)stream);
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "copy launch");
 }
 
