@@ -148,3 +148,24 @@ def test_cli_npy_reader_rejects_malformed_headers(tmp_path, raw, msg):
     bad.write_bytes(raw)
     r = _run("--image", str(img), "--binary", str(bad))
     assert r.returncode == 3 and msg in r.stderr, r.stderr
+
+
+@pytest.mark.parametrize("image,seed", [
+    (np.zeros((4, 5, 6), np.uint8), np.asfortranarray(np.zeros((4, 5, 6), np.int16))),
+    (np.zeros((1, 1, 4, 5, 6), np.float64), np.zeros((4, 5, 6), np.bool_)),
+    (np.asfortranarray(np.ones((4, 5, 6), np.float32)), np.zeros((1, 4, 5, 6), np.uint16)),
+])
+def test_cli_npy_reader_accepts_layouts_and_numeric_types(tmp_path, image, seed):
+    """Fortran order, leading size-1 axes and any integer, bool or float type
+    load; the run then either evolves (with a GPU) or stops at the device
+    (without one), never at the files."""
+    np.save(tmp_path / "img.npy", image)
+    np.save(tmp_path / "seed.npy", seed)
+    out = tmp_path / "phi.npy"
+    r = _run("--image", str(tmp_path / "img.npy"), "--binary", str(tmp_path / "seed.npy"), "--ouput", str(out),
+             "--t", "1", "--sigma", "1", "--quiet")
+    assert r.returncode in (0, 3), r.stderr
+    if r.returncode == 0:
+        assert np.load(out).shape == (4, 5, 6)
+    else:
+        assert str(tmp_path) not in r.stderr and "npy" not in r.stderr, r.stderr
