@@ -169,3 +169,56 @@ def test_cli_npy_reader_accepts_layouts_and_numeric_types(tmp_path, image, seed)
         assert np.load(out).shape == (4, 5, 6)
     else:
         assert str(tmp_path) not in r.stderr and "npy" not in r.stderr, r.stderr
+
+
+_NPY_DUMP = r'''
+#include <cstdio>
+#include "npy_io.h"
+// Loads argv[1] with the rsf3d reader; writes L H W is_u8 on stdout's first
+// line, then saves the C-order data as float32 .npy to argv[2].
+int main(int argc, char **argv) {
+    rsf::NpyVolume v;
+    std::string e = rsf::npy_load(argv[1], v);
+    if (!e.empty()) { std::fprintf(stderr, "%s\n", e.c_str()); return 3; }
+    std::vector<float> f(v.is_u8 ? v.u8.size() : 0);
+    for (size_t i = 0; i < f.size(); i++) f[i] = (float)v.u8[i];
+    e = rsf::npy_save_f32(argv[2], v.is_u8 ? f.data() : v.f32.data(), v.W, v.H, v.L);
+    if (!e.empty()) { std::fprintf(stderr, "%s\n", e.c_str()); return 4; }
+    std::printf("%lld %lld %lld %d\n", (long long)v.L, (long long)v.H, (long long)v.W, (int)v.is_u8);
+    return 0;
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def npy_dump(tmp_path_factory):
+    d = tmp_path_factory.mktemp("npydump")
+    (d / "main.cpp").write_text(_NPY_DUMP)
+    exe = d / "npy_dump"
+    csrc = PKG / "csrc"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(csrc), str(d / "main.cpp"), str(csrc / "npy_io.cpp"),
+                        "-o", str(exe)], capture_output=True, text=True, timeout=120)
+    if r.returncode != 0:
+        pytest.skip("g++ unavailable: " + r.stderr[-200:])
+    return exe
+
+
+@pytest.mark.parametrize("arr", [
+    np.arange(4 * 5 * 6, dtype=np.uint8).reshape(4, 5, 6),
+    np.asfortranarray(np.arange(4 * 5 * 6, dtype=np.int16).reshape(4, 5, 6) - 60),
+    np.asfortranarray(np.arange(3 * 7 * 2, dtype=np.uint8).reshape(3, 7, 2)),
+    np.linspace(-1, 1, 2 * 3 * 4).reshape(1, 1, 2, 3, 4),
+    (np.arange(60).reshape(3, 4, 5) % 3 == 0),
+    np.arange(60, dtype=np.uint32).reshape(5, 4, 3) * 1000,
+])
+def test_npy_reader_values_match_numpy(tmp_path, npy_dump, arr):
+    """The rsf3d reader returns every value in C order (x fastest), also for
+    Fortran-ordered files, and squeezes leading axes of length 1."""
+    src, out = tmp_path / "in.npy", tmp_path / "out.npy"
+    np.save(src, arr)
+    r = subprocess.run([str(npy_dump), str(src), str(out)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    want = np.ascontiguousarray(arr.reshape(arr.shape[-3:]), dtype=np.float32)
+    L, H, W, is_u8 = (int(v) for v in r.stdout.split())
+    assert (L, H, W) == want.shape and is_u8 == (arr.dtype == np.uint8)
+    assert np.array_equal(np.load(out), want)
