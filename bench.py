@@ -486,10 +486,12 @@ def run_ours(args):
     # The stencil, x-pass and z-pass are bound by instruction issue, not HBM:
     # their issue-side roofline is warp instructions per second (the ncu
     # count per voxel times this launch's voxels over its live time) against
-    # 152 SMs x 4 schedulers x one warp instruction per cycle at the SM clock.
+    # the SMs x 4 schedulers x one warp instruction per cycle at the SM clock.
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
     ipv = ncu_warp_inst_per_voxel(dom)
     if ipv is not None:
-        issue_peak = 152 * 4 * (clk.get("sm_mhz") or 2070.0) * 1e6
+        issue_peak = n_sm * 4 * sm_mhz * 1e6
         achieved = ipv * total_vox / (dk["ms_per_launch"] / 1e3)
         roofline["issue"] = {"warp_inst_per_voxel": ipv, "achieved_warp_inst_per_s": achieved,
                              "peak_warp_inst_per_s": issue_peak, "frac": achieved / issue_peak,
@@ -523,10 +525,10 @@ def run_ours(args):
         }
         # FP32 work of the separable 4-field schedule: 4 fields x 3 axes x k
         # FMAs (2 flops each) plus ~120 pointwise flops per voxel-iteration,
-        # against the non-tensor FP32 rate of 152 SMs x 128 lanes x 2 flops at
+        # against the non-tensor FP32 rate of the SMs x 128 lanes x 2 flops at
         # the SM clock seen during the timed region (a nominal figure).
         f_alg = 24 * k + 120
-        fp32_peak = 152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
+        fp32_peak = n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12
         line["fp32"] = {"flops_per_voxel_iter": f_alg, "achieved_tflops": value * f_alg / 1e3,
                         "nominal_peak_tflops": fp32_peak, "frac": value * f_alg / 1e3 / world / fp32_peak}
         if world == 1:

@@ -167,15 +167,17 @@ rsf_status rsf_set_kernel_timing(rsf_workspace *ws, int enable);
 rsf_status rsf_kernel_times(rsf_workspace *ws, double ms[4], int64_t launches[4], int reset);
 
 /* Evolution without any device allocation, for callers that cannot
- * allocate once running: work recorded into a CUDA stream capture (an
- * allocation cannot be captured), plug-ins inside an application that owns
- * the device memory through its own pool, real-time loops that forbid
+ * allocate once running: plug-ins inside an application that owns the
+ * device memory budget through its own pool, real-time loops that forbid
  * allocation after start-up.  Same arguments and result as rsf_evolve, but
  * no workspace: all scratch lives in one static device array of this
  * library (about 36 MiB), reserved when its module loads on a device and
  * held until the process exits.  Limit: W*H*L <= 1048576 voxels; larger
  * volumes return RSF_ERR_WORKSPACE_TOO_SMALL.  The first call on a device
- * looks up the array's device address (make it before any stream capture).
+ * looks up the array's device address and configures the kernels; make it
+ * before any stream capture (a first call on a capturing stream returns
+ * RSF_ERR_UNSUPPORTED).  The address is cached for the process: calls after
+ * cudaDeviceReset on that device are not supported.
  * Every call shares the array and finds the previous call's contents in it;
  * calls whose work overlaps on one GPU (for instance on two streams) race on
  * the array and corrupt each other: serialise them.  Non-finite values are

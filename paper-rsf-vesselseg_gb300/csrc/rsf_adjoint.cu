@@ -436,8 +436,8 @@ __global__ void adj_gather(AdjConst c, const float *wx, const float *wy, const f
 }
 
 unsigned blocks_for(long long n) {
-    const long long b = (n + kThreads - 1) / kThreads;
-    return (unsigned)(b < 152LL * 64 ? (b > 0 ? b : 1) : 152LL * 64);
+    const long long b = (n + kThreads - 1) / kThreads, cap = 64LL * sm_count();
+    return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
 }  // namespace

@@ -291,8 +291,8 @@ rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
 }
 
 // Lays out a batch in the workspace pools and uploads the table.
-rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, rsf_dtype dtype,
-                   const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, int *zc,
+rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, int box,
+                   rsf_dtype dtype, const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, int *zc,
                    cudaStream_t st) {
     if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
     if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
@@ -343,7 +343,14 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         d.db = d.xb;  // the data factor reuses the x-pass storage
         d.yb = ws->pool_y + off_y;
         off_v += nv;
-        off_x += 4 * (size_t)d.Wp * d.H * d.L;
+        // x-pass slot: the four x-pass fields, or with the box e-term f_out,
+        // f_in of the valid region followed by the data factor of every voxel
+        // (rounded up to 4 floats for the vector accesses).  Both are at most
+        // 4 W H L floats (Wp < W since k >= 5), so the pool of 4 max_voxels
+        // floats holds every batch that passes the voxel check above.
+        size_t slot_x = 4 * (size_t)d.Wp * d.H * d.L;
+        if (box > 0) slot_x = std::max(slot_x, (2 * (size_t)d.Wp * d.Hv * d.Lv + nv + 3) & ~(size_t)3);
+        off_x += slot_x;
         off_y += 4 * (size_t)d.Wp * d.Hv * d.L;
         for (int j = 0; j < rsf::NKERN; j++) {
             const int64_t next = (int64_t)pre[j * n1 + i] + tiles[j];
@@ -443,8 +450,8 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
     int tot[rsf::NKERN], xb_w = 0, zc = 0;
-    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), dtype, nullptr, tot, &xb_w, &zc,
-                st);
+    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), (int)p->sigma2, dtype, nullptr, tot,
+                &xb_w, &zc, st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
     const StepConst c = make_const(p, k, taps, dtype, n, xb_w, zc);
@@ -559,7 +566,7 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     const float *outs[1] = {phi_out};
     int tot[rsf::NKERN], xb_w = 0, zc = 0;
     cudaStream_t st = (cudaStream_t)stream;
-    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), dtype, outs, tot, &xb_w, &zc, st);
+    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), (int)p->sigma2, dtype, outs, tot, &xb_w, &zc, st);
     if (s != RSF_OK) return s;
     const StepConst c = make_const(p, k, taps, dtype, 1, xb_w, zc);
     const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};

@@ -31,11 +31,12 @@ cudaError_t launch_copy(void *dst, const void *src, size_t bytes, cudaStream_t s
     if (bytes == 0) return cudaSuccess;
     const uintptr_t a = reinterpret_cast<uintptr_t>(dst), b = reinterpret_cast<uintptr_t>(src);
     size_t head = 0;
+    const size_t max_blocks = 8 * (size_t)sm_count();
     if ((a & 15) == 0 && (b & 15) == 0) {
         const size_t n16 = bytes / 16;
         if (n16 > 0) {
             size_t blocks = (n16 + 511) / 512;
-            if (blocks > 152 * 8) blocks = 152 * 8;
+            if (blocks > max_blocks) blocks = max_blocks;
             copy16_kernel<<<(unsigned)blocks, 512, 0, st>>>(static_cast<const uint4 *>(src), static_cast<uint4 *>(dst),
                                                             n16);
         }
@@ -44,7 +45,7 @@ cudaError_t launch_copy(void *dst, const void *src, size_t bytes, cudaStream_t s
     const size_t rest = bytes - head;
     if (rest > 0) {
         size_t blocks = (rest + 255) / 256;
-        if (blocks > 152 * 8) blocks = 152 * 8;
+        if (blocks > max_blocks) blocks = max_blocks;
         copy1_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const unsigned char *>(src) + head,
                                                        static_cast<unsigned char *>(dst) + head, rest);
     }

@@ -89,6 +89,10 @@ cudaError_t launch_step(const SubVolDev *d_svs, const int *d_pre, const int *h_t
 
 cudaError_t configure_device();
 
+// Streaming multiprocessors of the current device (cached per device; 152 on
+// GB300), for grid caps and wave counts.
+int sm_count();
+
 // Sets the message rsf_last_error() returns on the calling thread.
 void set_last_error(const char *msg);
 

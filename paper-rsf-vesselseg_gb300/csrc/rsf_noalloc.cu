@@ -4,13 +4,13 @@
 // scratch (the second level-set buffer, the x- and y-pass fields, the batch
 // table and the error flag) lives in one file-scope device array of fixed
 // size instead of a caller-created workspace.  It is meant for callers that
-// must not allocate device memory once they are running: code that records
-// its work into a CUDA stream capture (an allocation cannot be captured),
-// plug-ins hosted by an application that owns the device memory budget
-// through its own pool, and real-time loops that forbid allocation after
-// start-up.  The array is reserved when this file's module is loaded on a
-// device (with CUDA's default lazy loading, at the first call on that
-// device) and is held until the process exits.
+// must not allocate device memory once they are running: plug-ins hosted by
+// an application that owns the device memory budget through its own pool,
+// and real-time loops that forbid allocation after start-up.  The array is
+// reserved when this file's module is loaded on a device (with CUDA's
+// default lazy loading, at the first call on that device) and is held until
+// the process exits.  Its device address is looked up once per device and
+// cached, so calls after cudaDeviceReset on that device are not supported.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -45,8 +45,10 @@ rsf_status fail(rsf_status s, const char *msg) {
 
 // Device address of the scratch array on the current device.  The host-side
 // name g_scratch is not a device address, so it is looked up once per device
-// (with that device current) and cached.
-rsf_status scratch_for_current_device(unsigned char **out) {
+// (with that device current) and cached.  The look-up and the kernel
+// configuration are not stream work, so a first call made while `st` is
+// capturing is refused instead of running them inside the capture.
+rsf_status scratch_for_current_device(cudaStream_t st, unsigned char **out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
@@ -54,6 +56,14 @@ rsf_status scratch_for_current_device(unsigned char **out) {
     }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_ptr[dev]) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(RSF_ERR_CUDA, "rsf_evolve_noalloc: cannot query the stream's capture status");
+        }
+        if (cap != cudaStreamCaptureStatusNone)
+            return fail(RSF_ERR_UNSUPPORTED,
+                        "rsf_evolve_noalloc: the first call on a device must not be made on a capturing stream");
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
         if (e != cudaSuccess || p == nullptr) {
@@ -94,8 +104,9 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     int k = 0;
     rsf_status s = rsf_gaussian_taps(p->sigma, taps, rsf::MAXK, &k);
     if (s != RSF_OK) return fail(s, "rsf_evolve_noalloc: invalid sigma");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     unsigned char *base = nullptr;
-    s = scratch_for_current_device(&base);
+    s = scratch_for_current_device(st, &base);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
 
@@ -151,7 +162,6 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     c.xb_w = xb_w;
     c.zc = zc;
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     // The table copies come from pageable host memory: they return once the
     // driver has staged the bytes, so the stack buffers may go out of scope.
     cudaError_t e = cudaMemcpyAsync(d_table, &d, sizeof d, cudaMemcpyHostToDevice, st);

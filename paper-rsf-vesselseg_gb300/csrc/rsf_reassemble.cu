@@ -121,7 +121,7 @@ cudaError_t launch_reassemble(const TileDev *d_tiles, const int n[3], const int 
     }
     const long long N = (long long)W * H * L;
     long long blocks = (N + kThreads - 1) / kThreads;
-    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    if (blocks > 32LL * sm_count()) blocks = 32LL * sm_count();
     reassemble_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(c, d_tiles, out);
     return cudaGetLastError();
 }

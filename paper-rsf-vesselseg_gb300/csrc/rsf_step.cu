@@ -2,9 +2,29 @@
 // sequence x-pass -> y-pass -> z-pass -> stencil.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "rsf_internal.h"
 
 namespace rsf {
+
+int sm_count() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return 1;
+    }
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
 
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp) {
     Wv = W - k + 1;
@@ -31,13 +51,13 @@ int choose_xb(const int *Wv, int n) {
 }
 
 // Stencil planes per block: ST_ZC, or half of it when the batch would then
-// give fewer than four waves of blocks (two resident per SM on 152 SMs).
+// give fewer than four waves of blocks (two resident per SM).
 int choose_zc(const int *whl, int n) {
     long long blocks = 0;
     for (int i = 0; i < n; i++)
         blocks += (long long)((whl[3 * i] + ST_OX - 1) / ST_OX) * ((whl[3 * i + 1] + ST_OY - 1) / ST_OY) *
                   ((whl[3 * i + 2] + ST_ZC - 1) / ST_ZC);
-    return blocks >= 4LL * 2 * 152 ? ST_ZC : ST_ZC / 2;
+    return blocks >= 4LL * 2 * sm_count() ? ST_ZC : ST_ZC / 2;
 }
 
 void tile_counts(const SubVolDev &d, int kspec, int xb_w, int zc, int tiles[NKERN]) {

@@ -1,7 +1,7 @@
 """A small, self-contained evolution for profiler captures.
 
-    python paper-rsf-vesselseg_gb300/rsf_gb300/profile_case.py --n 320 --sigma 3 --iters 2
-    python paper-rsf-vesselseg_gb300/rsf_gb300/profile_case.py --n 128 --sigma 3 --iters 1 --adjoint 2
+    python profile_case.py --n 320 --sigma 3 --iters 2
+    python profile_case.py --n 128 --sigma 3 --iters 1 --adjoint 2
 
 Evolves one n^3 volume (a smooth level set and a random uint8 image, made on
 the device) for `iters` iterations through the C ABI and exits.  At n = 320
@@ -15,7 +15,7 @@ import argparse
 import sys
 from pathlib import Path
 
-sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+sys.path.insert(0, str(Path(__file__).resolve().parent / "paper-rsf-vesselseg_gb300"))
 
 
 def main():

@@ -146,6 +146,36 @@ def test_batched_matches_plain(ws_big, cuda):
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("sigma2", [1.0, 2.0])
+def test_batched_box_e_term_matches_plain_and_oracle(sigma2, orc, ws_big, cuda):
+    """Batches with the box e-term, including a thin sub-volume (4 valid x
+    columns) before a larger one and an all-border one: each sub-volume's
+    scratch holds its fits and the data factor of every voxel without
+    reaching into the next sub-volume's."""
+    import torch
+    from rsf_gb300 import Params
+
+    shapes = [(64, 64, 24), (9, 9, 9), (40, 44, 48), (64, 64, 64)]
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=0.5, nu=65.025, eps=1.0, sigma2=sigma2)
+    iters = 2
+    inputs, pairs, plain = [], [], []
+    for i, s in enumerate(shapes):
+        img, phi0, _ = _inputs(s, seed=20 + i)
+        inputs.append((img, phi0))
+        ti = torch.from_numpy(img).to(cuda)
+        pairs.append((ti, torch.from_numpy(phi0).to(cuda)))
+        tp = torch.from_numpy(phi0).to(cuda)
+        ws_big.evolve(ti, tp, p, iters)
+        plain.append(tp)
+    ws_big.evolve_batched(pairs, p, iters)
+    ws_big.check()
+    for (img, phi0), (_, b), a in zip(inputs, pairs, plain):
+        got = b.cpu().numpy()
+        assert _bits_equal(got, a.cpu().numpy()), f"shape {img.shape}: batched differs from plain"
+        want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), iters)
+        assert _bits_equal(got, want), f"shape {img.shape}: {_diff_report(got, want)}"
+
+
 @pytest.mark.parametrize("eps", [1.0, 0.2])
 def test_config0_full_evolution_bit_exact(eps, orc, ws_big, cuda):
     """128^3 volume, 12 tubes, sigma 3, lambda 1, mu 1, nu 0.001*255^2, dt 0.1, 100 iterations."""

@@ -1,9 +1,10 @@
 """The allocation-free entry point (rsf_evolve_noalloc) against rsf_evolve.
 
 rsf_evolve_noalloc serves callers that cannot allocate device memory while
-running (work recorded into a stream capture, plug-ins inside an application
-that owns the device memory, real-time loops): it keeps its scratch in one
-static device array of the library instead of a workspace.  This test calls
+running (plug-ins inside an application that owns the device memory budget
+through its own pool, real-time loops that forbid allocation after start-up):
+it keeps its scratch in one static device array of the library instead of a
+workspace.  This test calls
 it through the C ABI twice in a row, on two different volumes, so that the
 second call runs on the scratch contents the first call left behind, and
 requires each result to be bit-identical to the workspace entry point's
