@@ -64,14 +64,18 @@ def dist_env():
 
 
 def algorithmic_bytes(tiles, k):
+    return algorithmic_bytes_shapes([t.shape for t in tiles], k)
+
+
+def algorithmic_bytes_shapes(shapes, k):
     """Bytes each kernel must move once per launch over the whole batch:
     x-pass reads phi (4) and I (1) and writes 4 fields of the x-valid extent;
     y-pass reads those and writes 4 fields of the xy-valid extent; z-pass
     reads those and I and writes the data factor of the valid region; the
     stencil reads phi and the data factor and writes phi."""
     out = {"xpass": 0, "ypass": 0, "zpass": 0, "stencil": 0}
-    for t in tiles:
-        L, H, W = t.shape
+    for shape in shapes:
+        L, H, W = shape
         Wv, Hv, Lv = max(W - k + 1, 0), max(H - k + 1, 0), max(L - k + 1, 0)
         if min(Wv, Hv, Lv) == 0:
             Wv = Hv = Lv = 0
@@ -252,31 +256,63 @@ def run_reference(args):
     return 0
 
 
+def _config0_volume(seed):
+    """One 128^3 volume of the 128^3 generator (CPU, per-region perturbation)."""
+    from rsf_gb300 import synth
+
+    return synth.make_volume(synth.VolumeSpec((128, 128, 128), 12, 2.0, 6.0, seed))
+
+
 def differentiable_sample(dev):
-    """The differentiable workload: 8 volumes of 128^3 (the 128^3 generator),
-    50 forward iterations with checkpoints every 10, soft-Dice loss against
-    the true mask, backward through the hand-written adjoint.  Returns the
-    forward + backward time per batch and the throughput in forward
-    voxel-iterations per second of the whole forward + backward job."""
+    """The differentiable workload as specified: a batch of 8 volumes of
+    128^3 from the 128^3 generator (seeds 40-47; uint8 image in 0-255,
+    phi0 the +-3-clipped signed distance of the perturbed mask), sigma 3,
+    lambda1 = lambda2 = 1, mu 1, nu 0.001*255^2, eps 1, dt 0.1, 50 forward
+    iterations with checkpoints every 10, loss = mean soft-Dice of H(phi_T)
+    against the true tube mask, backward through the hand-written adjoint;
+    gradients of phi0 and of lambda1, lambda2, mu, nu.  Returns the forward +
+    backward time per batch and the throughput in forward voxel-iterations
+    per second of the whole forward + backward job.
+
+    At this phi0 the exact 50-step gradient overflows FP32: where the
+    clipped distance is flat, n = g/(|g| + 1e-6) has derivative 1e6 and each
+    step multiplies the gradient by up to ~1e5 (the float64 restatement
+    measures ~1e80).  The kernels run the same work either way; the record
+    says whether the workspace check reported the overflow."""
+    import multiprocessing as mp
+
     import torch
 
-    from rsf_gb300 import Params, Workspace, autograd, synth
+    from rsf_gb300 import Params, RsfError, Workspace, autograd
 
-    p = Params(sigma=3.0, dt=0.1, mu=0.2, lambda1=1.0, lambda2=1.0, nu=0.1, eps=1.0)
-    vols = []
-    for b in range(8):
-        spec = synth.VolumeSpec((128, 128, 128), 12, 2.0, 6.0, 40 + b)
-        img, phi0, mask = synth.make_volume_torch(spec, dev)
-        vols.append(((img.float() / 255.0).contiguous(), phi0, mask))
+    # the generator is CPU-bound: one spawned process per volume
+    with mp.get_context("spawn").Pool(8) as pool:
+        vols_np = pool.map(_config0_volume, range(40, 48))
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=0.001 * 255.0 ** 2, eps=1.0)
+    vols = [(torch.from_numpy(img).to(dev), torch.from_numpy(phi0).to(dev), torch.from_numpy(mask).to(dev))
+            for img, phi0, mask in vols_np]
     ws = Workspace(128 ** 3)
+    names = ("lambda1", "lambda2", "mu", "nu")
+    grads = {}
 
     def batch():
-        for img, phi0, mask in vols:
-            x = phi0.clone().requires_grad_(True)
-            lam = torch.tensor(1.0, dtype=torch.float64, device=dev, requires_grad=True)
-            loss = autograd.soft_dice_loss(autograd.evolve(x, img, p, 50, lambda1=lam, checkpoint_every=10,
-                                                           workspace=ws), mask, p.eps)
-            loss.backward()
+        # parameter leaves on the host: reading their values costs no device sync
+        prm = {n: torch.tensor(float(getattr(p, n)), dtype=torch.float64, requires_grad=True) for n in names}
+        xs = [phi0.clone().requires_grad_(True) for _, phi0, _ in vols]
+        loss = 0.0
+        for (img, _, mask), x in zip(vols, xs):
+            out = autograd.evolve(x, img, p, 50, checkpoint_every=10, workspace=ws, **prm)
+            loss = loss + autograd.soft_dice_loss(out, mask, p.eps)
+        (loss / len(vols)).backward()
+        grads["phi0_l2"] = float(torch.sqrt(sum((x.grad.double() ** 2).sum() for x in xs)))
+        for n in names:
+            grads[n] = float(prm[n].grad)
+        grads["loss"] = float(loss) / len(vols)
+        try:
+            ws.check()
+            grads["check"] = "ok"
+        except RsfError as err:
+            grads["check"] = str(err)
 
     batch()
     torch.cuda.synchronize()
@@ -287,10 +323,138 @@ def differentiable_sample(dev):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     ws.close()
-    return {"workload": "8 x 128^3, 50 iterations, checkpoints every 10, soft-Dice loss, gradients of phi0 and "
-                        "lambda1 (image scaled to [0, 1], mu 0.2, nu 0.1, eps 1, sigma 3)",
+    num = {k: v for k, v in grads.items() if isinstance(v, float)}
+    finite = all(v == v and abs(v) != float("inf") for v in num.values())
+    # JSON has no NaN or infinity: non-finite values are reported as null
+    grads = {k: (v if not isinstance(v, float) or (v == v and abs(v) != float("inf")) else None)
+             for k, v in grads.items()}
+    return {"workload": "config4: 8 x 128^3 (128^3 generator, seeds 40-47, uint8 image 0-255, phi0 the +-3-clipped "
+                        "signed distance), sigma 3, lambda1 = lambda2 = 1, mu 1, nu 0.001*255^2, eps 1, dt 0.1, "
+                        "50 iterations, checkpoints every 10, mean soft-Dice loss; gradients of phi0, lambda1, "
+                        "lambda2, mu, nu",
             "fwd_bwd_ms_per_batch": ms, "value": 8 * 128 ** 3 * 50 / (ms / 1e3) / 1e9,
-            "unit": "forward Gvoxel-iter/s through forward + backward"}
+            "unit": "forward Gvoxel-iter/s through forward + backward",
+            "gradients": grads, "gradients_finite": finite}
+
+
+def _timed_evolutions(ws, pairs, p, iters, steps, batched):
+    """Device time of `steps` evolutions of `iters` iterations (each from the
+    same start, restored before the call) and the per-kernel times."""
+    import torch
+
+    starts = [phi.clone() for _, phi in pairs]
+
+    def one():
+        for (_, phi), s in zip(pairs, starts):
+            phi.copy_(s)
+        if batched:
+            ws.evolve_batched(pairs, p, iters)
+        else:
+            for im, phi in pairs:
+                ws.evolve(im, phi, p, iters)
+
+    ws.set_kernel_timing(True)
+    ws.kernel_times(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = 0.0
+    for _ in range(steps):
+        one()
+        torch.cuda.synchronize()
+        e0.record()
+        if batched:
+            ws.evolve_batched(pairs, p, iters)
+        else:
+            for im, phi in pairs:
+                ws.evolve(im, phi, p, iters)
+        e1.record()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    kt = ws.kernel_times(reset=True)
+    ws.set_kernel_timing(False)
+    ws.check()
+    del starts
+    return ms / steps, kt
+
+
+def _kernel_summary(kt, alg):
+    out = {}
+    tot = sum(v[0] for v in kt.values())
+    for name, (kms, nl) in kt.items():
+        if nl:
+            per = kms / nl
+            out[name] = {"ms_per_launch": per, "share": kms / max(tot, 1e-9),
+                         "gbs": alg[name] / (per / 1e3) / 1e9}
+    return out
+
+
+def config1_sample(dev, peak):
+    """One 512^3 uint8 volume (200 tubes, radius U[1.5, 8]), sigma 3 and 5,
+    200 iterations through rsf_evolve (the single-volume path): value, the
+    per-kernel times and the step's HBM fraction."""
+    import torch
+
+    from rsf_gb300 import Params, Workspace, gaussian_taps, synth
+
+    img, phi0, _ = synth.make_volume_torch(synth.CONFIG1, dev)
+    n = img.numel()
+    out = {"workload": "config1: one 512^3 uint8 volume (200 tubes, radius U[1.5,8]), lambda 1, mu 1, "
+                       "nu 0.001*255^2, eps 1, dt 0.1, 200 iterations, rsf_evolve", "unit": UNIT}
+    ws = Workspace(n)
+    for sigma in (3.0, 5.0):
+        p = Params(**dict(PARAMS, sigma=sigma))
+        k = len(gaussian_taps(sigma))
+        phi = phi0.clone()
+        pairs = [(img, phi)]
+        ws.evolve(img, phi, p, 10)  # warm-up
+        phi.copy_(phi0)
+        ms, kt = _timed_evolutions(ws, pairs, p, 200, 1, batched=False)
+        alg = algorithmic_bytes_shapes([tuple(img.shape)], k)
+        value = n * 200 / (ms / 1e3) / 1e9
+        out[f"sigma{int(sigma)}"] = {
+            "taps": k, "value": value, "ms_per_iteration": ms / 200,
+            "step_alg_bytes_per_voxel_iter": sum(alg.values()) / n,
+            "step_hbm_frac": sum(alg.values()) * 200 / (ms / 1e3) / 1e9 / peak,
+            "kernels": _kernel_summary(kt, alg)}
+        del phi, pairs
+    ws.close()
+    del img, phi0
+    torch.cuda.empty_cache()
+    return out
+
+
+def gigavoxel_sample(dev, peak):
+    """The gigavoxel batch: the 1024^3 volume (2000 tubes, radius U[1, 10]) in
+    27 tiles of 384/384/256 cores + 32-voxel halos (1.53 G tile voxels, all
+    resident in HBM), sigma 4, 200 iterations, batched and one at a time."""
+    import torch
+
+    from rsf_gb300 import Params, Workspace, gaussian_taps, synth, tiling
+
+    img_full, phi_full, _ = synth.make_volume_torch(synth.CONFIG3, dev)
+    tiles = tiling.config3_tiles()
+    imgs = [img_full[t.slices()].contiguous() for t in tiles]
+    phis = [phi_full[t.slices()].contiguous() for t in tiles]
+    del img_full, phi_full
+    torch.cuda.empty_cache()
+    total = sum(t.voxels for t in tiles)
+    p = Params(**dict(PARAMS, sigma=4.0))
+    k = len(gaussian_taps(4.0))
+    ws = Workspace(total, len(tiles))
+    pairs = list(zip(imgs, phis))
+    ws.evolve_batched(pairs, p, 4)  # warm-up
+    ms, kt = _timed_evolutions(ws, pairs, p, 200, 2, batched=True)
+    plain_ms, _ = _timed_evolutions(ws, pairs, p, 200, 1, batched=False)
+    alg = algorithmic_bytes(tiles, k)
+    value = total * 200 / (ms / 1e3) / 1e9
+    ws.close()
+    del pairs, imgs, phis
+    torch.cuda.empty_cache()
+    return {"workload": "config3: 27 sub-volumes (384/384/256 cores + 32-voxel halos, extents 288-448) of a 1024^3 "
+                        "synthetic vessel volume (2000 tubes, radius U[1,10]); sigma 4 (29 taps), 200 iterations",
+            "voxels": total, "unit": UNIT, "value": value, "ms_per_step": ms, "steps": 2,
+            "plain": total * 200 / (plain_ms / 1e3) / 1e9, "batched_vs_plain": plain_ms / ms,
+            "step_hbm_frac": sum(alg.values()) * 200 / (ms / 1e3) / 1e9 / peak,
+            "kernels": _kernel_summary(kt, alg)}
 
 
 def run_ours(args):
@@ -532,10 +696,18 @@ def run_ours(args):
         line["fp32"] = {"flops_per_voxel_iter": f_alg, "achieved_tflops": value * f_alg / 1e3,
                         "nominal_peak_tflops": fp32_peak, "frac": value * f_alg / 1e3 / world / fp32_peak}
         if world == 1:
+            # the other workloads, after the headline's buffers are released
+            ws.close()
+            del sets, h_img, h_phi, h_out
+            torch.cuda.empty_cache()
             base, sample = cpu_sample(os.cpu_count() or 1)
             line["cpu_baseline"] = base
             line["parity"] = parity_on_sample(sample)
-            line["differentiable"] = differentiable_sample(dev)
+            if not args.headline_only:
+                line["config1"] = config1_sample(dev, peak)
+                if args.workload == "config2":
+                    line["gigavoxel"] = gigavoxel_sample(dev, peak)
+                line["differentiable"] = differentiable_sample(dev)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -548,6 +720,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the 512^3, gigavoxel and differentiable records after the headline")
     ap.add_argument("--workload", choices=["config2", "gigavoxel"], default="config2",
                     help="config2 (default, the 48-sub-volume batch) or gigavoxel (1024^3 in 27 tiles)")
     args = ap.parse_args()

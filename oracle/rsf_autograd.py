@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 
-def _neighbours(shape, boundary=0):
+def _neighbours(shape, boundary=0, device=None):
     """(right, left) flat index arrays of the central difference on each axis."""
     L, H, W = shape
     idx = np.arange(L * H * W, dtype=np.int64).reshape(L, H, W)
@@ -40,7 +40,7 @@ def _neighbours(shape, boundary=0):
         qr = np.minimum(q + 1, n - 1)
         ql = np.maximum(q - 1, 0)
         out.append(((idx + (qr - q) * stride).ravel(), (idx + (ql - q) * stride).ravel()))
-    return [(torch.from_numpy(a), torch.from_numpy(b)) for a, b in out]
+    return [(torch.from_numpy(a).to(device), torch.from_numpy(b).to(device)) for a, b in out]
 
 
 def _blur_valid(f, taps):
@@ -54,15 +54,16 @@ def _blur_valid(f, taps):
 
 
 class Step:
-    """phi' = step(phi, I, lambda1, lambda2, mu, nu) for one volume shape."""
+    """phi' = step(phi, I, lambda1, lambda2, mu, nu) for one volume shape;
+    `device` is where its index and tap tensors live (that of phi and I)."""
 
-    def __init__(self, shape, taps, dt, eps, boundary=0):
+    def __init__(self, shape, taps, dt, eps, boundary=0, device=None):
         self.shape = tuple(shape)
-        self.taps = torch.as_tensor(np.asarray(taps, dtype=np.float64))
+        self.taps = torch.as_tensor(np.asarray(taps, dtype=np.float64)).to(device)
         self.k = self.taps.numel()
         self.r = (self.k - 1) // 2
         self.dt, self.eps = float(dt), float(eps)
-        self.nb = _neighbours(self.shape, boundary)
+        self.nb = _neighbours(self.shape, boundary, device)
 
     def _d(self, f, axis):
         r, l = self.nb[axis]
@@ -100,7 +101,7 @@ class Step:
 def evolve(phi0, I, taps, params: dict, iters: int, boundary=0):
     """phi_T in float64 with autograd through every step.  params: dt, eps,
     lambda1, lambda2, mu, nu (the last four floats or float64 tensors)."""
-    step = Step(phi0.shape, taps, params["dt"], params["eps"], boundary)
+    step = Step(phi0.shape, taps, params["dt"], params["eps"], boundary, phi0.device)
     phi = phi0
     for _ in range(iters):
         phi = step(phi, I, params["lambda1"], params["lambda2"], params["mu"], params["nu"])

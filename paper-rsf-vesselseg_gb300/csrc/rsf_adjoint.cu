@@ -421,8 +421,9 @@ __global__ void adj_w(AdjConst c, const float *phi, const float *u, const float 
     }
 }
 
-// out += sum_a D_a^T w_a.
-__global__ void adj_gather(AdjConst c, const float *wx, const float *wy, const float *wz, float *out) {
+// out += sum_a D_a^T w_a; a non-finite result sets kFlagAdjointNonFinite.
+__global__ void adj_gather(AdjConst c, const float *wx, const float *wy, const float *wz, float *out,
+                           unsigned *flag) {
     const long long N = (long long)c.W * c.H * c.L;
     const long long plane = (long long)c.W * c.H;
     auto vx = [&](long long m) { return wx[m]; };
@@ -431,7 +432,9 @@ __global__ void adj_gather(AdjConst c, const float *wx, const float *wy, const f
     const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y, z = blockIdx.z;
     if (x < c.W && y < c.H) {
         const long long i = ((long long)z * c.H + y) * c.W + x;
-        out[i] += dT_x(c, i, x, N, vx) + dT_axis(i, y, c.H, c.W, vy) + dT_axis(i, z, c.L, plane, vz);
+        const float v = out[i] + (dT_x(c, i, x, N, vx) + dT_axis(i, y, c.H, c.W, vy) + dT_axis(i, z, c.L, plane, vz));
+        out[i] = v;
+        if (!isfinite(v) && flag) atomicOr(flag, kFlagAdjointNonFinite);
     }
 }
 
@@ -451,7 +454,7 @@ unsigned blocks_for(long long n) {
 cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,
                                 int boundary, int img_f32, const float *phi, const void *img, const float *u,
                                 float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
-                                cudaStream_t st) {
+                                unsigned *flag, cudaStream_t st) {
     AdjConst c;
     for (int t = 0; t < MAXK; t++) c.taps[t] = t < k ? taps[t] : 0.0f;
     c.k = k;
@@ -498,7 +501,7 @@ cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, f
                   (unsigned)((L + kPointZ - 1) / kPointZ));
     adj_point<<<gp, b3, 0, st>>>(c, phi, img, u, gxb, gyb, gzb, nxb, nyb, nzb, hbar, eo, ei, out, grads);
     adj_w<<<g3, b3, 0, st>>>(c, phi, u, gxb, gyb, gzb, nxb, nyb, nzb, hbar, eo, ei);
-    adj_gather<<<g3, b3, 0, st>>>(c, hbar, eo, ei, out);
+    adj_gather<<<g3, b3, 0, st>>>(c, hbar, eo, ei, out, flag);
     return cudaGetLastError();
 }
 

@@ -49,6 +49,7 @@ struct rsf_workspace {
     float *pool_y = nullptr;     // y-pass fields, 4 * max_voxels
     SubVolDev *d_svs = nullptr;
     int *d_pre = nullptr;        // NKERN * (max_subvols + 1)
+    unsigned char *d_maps = nullptr;  // TMA maps of the pair planes, max_subvols * TMAP_BYTES
     unsigned *d_flag = nullptr;
     // Pinned staging of the table, kStages slots used in turn: a call waits
     // only for the upload of the call kStages before it, so consecutive
@@ -56,11 +57,12 @@ struct rsf_workspace {
     static constexpr int kStages = 4;
     SubVolDev *h_svs = nullptr;  // kStages * max_subvols
     int *h_pre = nullptr;        // kStages * NKERN * (max_subvols + 1)
+    unsigned char *h_maps = nullptr;  // kStages * max_subvols * TMAP_BYTES
     cudaEvent_t table_ev[kStages] = {};
     bool table_pending[kStages] = {};
     int stage = 0;
     // Staging slot for the next upload; waits until its previous upload is done.
-    cudaError_t next_stage(SubVolDev **svs, int **pre) {
+    cudaError_t next_stage(SubVolDev **svs, int **pre, unsigned char **maps) {
         if (table_pending[stage]) {
             cudaError_t e = cudaEventSynchronize(table_ev[stage]);
             if (e != cudaSuccess) return e;
@@ -68,6 +70,7 @@ struct rsf_workspace {
         }
         *svs = h_svs + (size_t)stage * max_subvols;
         *pre = h_pre + (size_t)stage * rsf::NKERN * ((size_t)max_subvols + 1);
+        *maps = h_maps + (size_t)stage * max_subvols * rsf::TMAP_BYTES;
         return cudaSuccess;
     }
     cudaError_t mark_stage(cudaStream_t st) {
@@ -184,7 +187,8 @@ rsf_status rsf_gaussian_taps(float sigma, float *taps, int cap, int *k_out) {
 size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols) {
     const size_t v = (size_t)std::max<int64_t>(max_voxels, 0);
     const size_t n = (size_t)std::max<int32_t>(max_subvols, 1);
-    return v * sizeof(float) * 9 + n * sizeof(SubVolDev) + rsf::NKERN * (n + 1) * sizeof(int) + 256;
+    return v * sizeof(float) * 9 + n * (sizeof(SubVolDev) + rsf::TMAP_BYTES) + rsf::NKERN * (n + 1) * sizeof(int) +
+           256;
 }
 
 static void ws_free(rsf_workspace *ws) {
@@ -199,11 +203,13 @@ static void ws_free(rsf_workspace *ws) {
     cudaFree(ws->pool_y);
     cudaFree(ws->d_svs);
     cudaFree(ws->d_pre);
+    cudaFree(ws->d_maps);
     cudaFree(ws->d_flag);
     cudaFree(ws->stage_img);
     cudaFree(ws->stage_phi);
     cudaFreeHost(ws->h_svs);
     cudaFreeHost(ws->h_pre);
+    cudaFreeHost(ws->h_maps);
     for (cudaEvent_t ev : ws->table_ev)
         if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : ws->events) cudaEventDestroy(ev);
@@ -235,11 +241,13 @@ rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_wor
     alloc((void **)&ws->pool_y, 4 * v * sizeof(float));
     alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
     alloc((void **)&ws->d_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
+    alloc((void **)&ws->d_maps, (size_t)max_subvols * rsf::TMAP_BYTES);
     alloc((void **)&ws->d_flag, 256);
     const size_t ns = rsf_workspace::kStages;
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, ns * (size_t)max_subvols * sizeof(SubVolDev));
     if (e == cudaSuccess)
         e = cudaMallocHost((void **)&ws->h_pre, ns * rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_maps, ns * (size_t)max_subvols * rsf::TMAP_BYTES);
     for (size_t i = 0; i < ns && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&ws->table_ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws->capture_stream, cudaStreamNonBlocking);
@@ -292,8 +300,8 @@ rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
 
 // Lays out a batch in the workspace pools and uploads the table.
 rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, int box,
-                   rsf_dtype dtype, const float *const *phi_out_override, int totals[rsf::NKERN], int *xb_w, int *zc,
-                   cudaStream_t st) {
+                   rsf_dtype dtype, const float *const *phi_out_override, int totals[rsf::NKERN],
+                   rsf::LaunchShape *shape, cudaStream_t st) {
     if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
     if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
@@ -307,21 +315,18 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
     if (total > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "batch larger than the workspace");
     SubVolDev *h_svs = nullptr;
     int *h_pre = nullptr;
+    unsigned char *h_maps = nullptr;
     {
-        cudaError_t e = ws->next_stage(&h_svs, &h_pre);
+        cudaError_t e = ws->next_stage(&h_svs, &h_pre, &h_maps);
         if (e != cudaSuccess) return cuda_fail(e, "table event");
     }
-    std::vector<int> wv(n), whl(3 * (size_t)n);
+    std::vector<int> whl(3 * (size_t)n);
     for (int i = 0; i < n; i++) {
-        int Wv, Hv, Lv, Wp;
-        rsf::valid_extents((int)svs[i].W, (int)svs[i].H, (int)svs[i].L, k, Wv, Hv, Lv, Wp);
-        wv[i] = Wv;
         whl[3 * i] = (int)svs[i].W;
         whl[3 * i + 1] = (int)svs[i].H;
         whl[3 * i + 2] = (int)svs[i].L;
     }
-    *xb_w = rsf::choose_xb(wv.data(), n);
-    *zc = rsf::choose_zc(whl.data(), n);
+    *shape = rsf::choose_shape(whl.data(), n, k, kspec);
     const int n1 = n + 1;
     int *pre = h_pre;
     for (int j = 0; j < rsf::NKERN; j++) pre[j * n1] = 0;
@@ -334,7 +339,7 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         d.L = (int)svs[i].L;
         rsf::valid_extents(d.W, d.H, d.L, k, d.Wv, d.Hv, d.Lv, d.Wp);
         int tiles[rsf::NKERN];
-        rsf::tile_counts(d, kspec, *xb_w, *zc, tiles);
+        rsf::tile_counts(d, kspec, *shape, tiles);
         const size_t nv = (size_t)d.W * d.H * d.L;
         d.phi[0] = svs[i].phi;
         d.phi[1] = phi_out_override ? const_cast<float *>(phi_out_override[i]) : ws->pool_phi2 + off_v;
@@ -358,17 +363,22 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
             pre[j * n1 + i + 1] = (int)next;
         }
         h_svs[i] = d;
+        if (shape->zt && d.Wv > 0 && !rsf::encode_pair_map(h_maps + (size_t)i * rsf::TMAP_BYTES, d))
+            return fail(RSF_ERR_CUDA, "TMA tensor map encoding of the pair planes failed");
     }
     for (int j = 0; j < rsf::NKERN; j++) totals[j] = pre[j * n1 + n];
     cudaError_t e = cudaMemcpyAsync(ws->d_svs, h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ws->d_pre, h_pre, rsf::NKERN * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && shape->zt)
+        e = cudaMemcpyAsync(ws->d_maps, h_maps, (size_t)n * rsf::TMAP_BYTES, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = ws->mark_stage(st);
     if (e != cudaSuccess) return cuda_fail(e, "table upload");
     return RSF_OK;
 }
 
-StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n, int xb_w, int zc) {
+StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dtype, int n,
+                     const rsf::LaunchShape &sh, const void *maps) {
     StepConst c;
     std::memset(&c, 0, sizeof c);
     for (int i = 0; i < k; i++) {
@@ -387,8 +397,10 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.boundary = p->boundary;
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
-    c.xb_w = xb_w;
-    c.zc = zc;
+    c.xb_w = sh.xb_w;
+    c.xy_tx = sh.xy_tx;
+    c.zc = sh.zc;
+    c.ymaps = sh.zt ? maps : nullptr;
     c.box = (int)p->sigma2;
     return c;
 }
@@ -449,12 +461,13 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     int k = 0;
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
-    int tot[rsf::NKERN], xb_w = 0, zc = 0;
+    int tot[rsf::NKERN];
+    rsf::LaunchShape sh;
     s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), (int)p->sigma2, dtype, nullptr, tot,
-                &xb_w, &zc, st);
+                &sh, st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
-    const StepConst c = make_const(p, k, taps, dtype, n, xb_w, zc);
+    const StepConst c = make_const(p, k, taps, dtype, n, sh, ws->d_maps);
     if (ws->timing) {
         s = timing_events(ws, iters, tot);
         if (s != RSF_OK) return s;
@@ -564,11 +577,12 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     if (s != RSF_OK) return s;
     rsf_subvol sv = {const_cast<float *>(phi), image, W, H, L};
     const float *outs[1] = {phi_out};
-    int tot[rsf::NKERN], xb_w = 0, zc = 0;
+    int tot[rsf::NKERN];
+    rsf::LaunchShape sh;
     cudaStream_t st = (cudaStream_t)stream;
-    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), (int)p->sigma2, dtype, outs, tot, &xb_w, &zc, st);
+    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), (int)p->sigma2, dtype, outs, tot, &sh, st);
     if (s != RSF_OK) return s;
-    const StepConst c = make_const(p, k, taps, dtype, 1, xb_w, zc);
+    const StepConst c = make_const(p, k, taps, dtype, 1, sh, ws->d_maps);
     const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};
     cudaError_t e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, 0, p->arith, ws->d_flag, &dbg, st);
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");
@@ -620,7 +634,7 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
     cudaError_t e = rsf::launch_step_adjoint(taps, k, p->eps, p->dt, p->mu, p->nu, p->lambda1, p->lambda2,
                                              p->boundary, dtype == RSF_F32, phi, image, phi_bar_in, phi_bar_out,
                                              param_grads, (int)W, (int)H, (int)L, ws->pool_phi2, ws->pool_x,
-                                             ws->pool_y, (cudaStream_t)stream);
+                                             ws->pool_y, ws->d_flag, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
     return RSF_OK;
 }
@@ -653,8 +667,9 @@ rsf_status rsf_reassemble(rsf_workspace *ws, const rsf_tile *tiles, int32_t nx, 
     }
     SubVolDev *h_svs = nullptr;
     int *h_pre = nullptr;
+    unsigned char *h_maps = nullptr;
     {
-        cudaError_t e = ws->next_stage(&h_svs, &h_pre);
+        cudaError_t e = ws->next_stage(&h_svs, &h_pre, &h_maps);
         if (e != cudaSuccess) return cuda_fail(e, "table event");
     }
     rsf::TileDev *h = reinterpret_cast<rsf::TileDev *>(h_svs);
@@ -712,6 +727,9 @@ rsf_status rsf_workspace_check(rsf_workspace *ws, void *stream) {
     e = cudaMemcpy(&flag, ws->d_flag, sizeof flag, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && flag) e = cudaMemset(ws->d_flag, 0, sizeof flag);
     if (e != cudaSuccess) return cuda_fail(e, "flag read");
+    if (flag & rsf::kFlagAdjointNonFinite)
+        return fail(RSF_ERR_NONFINITE, "non-finite value in dL/dphi from rsf_step_adjoint (the gradient overflowed FP32)");
+    if (flag & rsf::kFlagTimeout) return fail(RSF_ERR_CUDA, "a kernel's barrier wait gave up (TMA copy not completed)");
     if (flag) return fail(RSF_ERR_NONFINITE, "non-finite value written to phi");
     return RSF_OK;
 }

@@ -23,9 +23,17 @@ constexpr int ST_ZC = 64;      // stencil: planes per block (32 when that gives 
 // The x-pass lane width (outputs per lane) is chosen per launch from these.
 constexpr int XB_CHOICES[2] = {5, 9};
 
+// Fused x/y-pass (rsf_xy.cuh): rows per chunk, which must divide the tap
+// count, and the range of its tile width TX (a multiple of XY_R, chosen per
+// launch; the block has 2 TX threads).
+constexpr int XY_R = 7;
+constexpr int XY_TX_MIN = 84;
+constexpr int XY_TX_MAX = 154;
+
 // One sub-volume as the kernels see it.
 //   xb: 4 x-pass fields, each Wp x H x L   (row stride Wp)
-//   yb: 4 y-pass fields, each Wp x Hv x L
+//   yb: 4 y-pass fields, each Wp x Hv x L; after the fused x/y-pass two
+//       float2 pair planes (H, 1-H) and (I H, I (1-H)), each Wp x Hv x L
 //   db: data factor lambda (e_out - e_in) of the valid region, Wp x Hv x Lv;
 //       it reuses the x-pass storage, which is dead once the y-pass has run.
 //       With the box e-term it holds f_out and f_in of the valid region
@@ -54,9 +62,19 @@ struct StepConst {
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
     int xb_w;       // x-pass outputs per lane for this launch
+    int xy_tx;      // fused x/y-pass tile width for this launch (0: separate passes)
     int zc;         // stencil planes per block for this launch
     int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
+    const void *ymaps;  // fused path: per sub-volume TMA map of the pair planes (TMAP_BYTES each)
 };
+
+// TMA tensor maps (CUtensorMap) as the kernels see them: 128 bytes each, in
+// device memory aligned to 128 bytes.
+constexpr int TMAP_BYTES = 128;
+// Encodes the z-pass map of d's pair planes into `out` (host memory); false
+// when the driver's encoder is unavailable or refuses the layout.
+bool encode_pair_map(void *out, const SubVolDev &d);
+bool tensor_maps_available();
 
 // Optional per-voxel debug outputs (8 fields, full-volume layout).
 struct DebugOut {
@@ -64,7 +82,12 @@ struct DebugOut {
     int64_t n;
 };
 
-constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil
+constexpr int NKERN = 4;  // x-pass (or fused x/y-pass), y-pass, z-pass, stencil
+
+// Bits of the per-workspace error flag the kernels set.
+constexpr unsigned kFlagNonFinite = 1u;  // a non-finite value was written to phi
+constexpr unsigned kFlagTimeout = 2u;    // a barrier wait gave up (a TMA copy did not complete)
+constexpr unsigned kFlagAdjointNonFinite = 4u;  // rsf_step_adjoint produced a non-finite dL/dphi
 
 // Tap counts with streaming (compile-time K) kernels.  Other tap counts, the
 // debug step, the reference arithmetic and the box e-term use the
@@ -73,11 +96,23 @@ inline bool is_specialised(int k) { return k == 21 || k == 29 || k == 35; }
 inline int kernel_k(int k, int arith, bool debug, int box = 0) {
     return (is_specialised(k) && arith == 0 && !debug && box == 0) ? k : 0;
 }
+// Specialised tap counts whose x and y correlations run fused (XY_R | k).
+inline bool fused_xy(int kspec) { return kspec == 21 || kspec == 35; }
 constexpr int MAX_BOX = 8;  // largest e-term box radius
 
 // Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
-void tile_counts(const SubVolDev &d, int kspec, int xb_w, int zc, int tiles[NKERN]);
+// Per-launch tile shapes of a batch.
+struct LaunchShape {
+    int xb_w;   // x-pass outputs per lane (separate passes)
+    int xy_tx;  // fused x/y-pass tile width (0: separate passes)
+    int zt;     // 1: the fused path's z-pass loads planes with TMA (needs a map per sub-volume)
+    int zc;     // stencil planes per block
+};
+// whl: W, H, L of each sub-volume; kspec: kernel_k().
+LaunchShape choose_shape(const int *whl, int n, int k, int kspec);
+void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NKERN]);
 int choose_xb(const int *Wv, int n);
+int choose_xy_tx(const int *whl, int n, int k);
 int choose_zc(const int *whl, int n);  // whl: W, H, L of each sub-volume
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
 
@@ -108,6 +143,12 @@ RSF_DECLARE_K(21)
 RSF_DECLARE_K(29)
 RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
+cudaError_t launch_xypass_21(const SubVolDev *, const int *, int, const StepConst &, int parity, cudaStream_t);
+cudaError_t launch_xypass_35(const SubVolDev *, const int *, int, const StepConst &, int parity, cudaStream_t);
+cudaError_t config_xypass_21();
+cudaError_t config_xypass_35();
+cudaError_t launch_ztpass_21(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
+cudaError_t launch_ztpass_35(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
                            unsigned *flag, const DebugOut *dbg, cudaStream_t);
 // Box e-term (c.box >= 1): data factor of every voxel, stencil tiling.
@@ -117,7 +158,7 @@ cudaError_t launch_box(const SubVolDev *, const int *, int, const StepConst &, c
 cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,
                                 int boundary, int img_f32, const float *phi, const void *img, const float *u,
                                 float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
-                                cudaStream_t st);
+                                unsigned *flag, cudaStream_t st);
 // Reassembly (rsf_reassemble.cu): one evolved sub-volume placed in the output.
 constexpr int RA_MAXCELLS = 64;  // grid cells per axis
 struct TileDev {

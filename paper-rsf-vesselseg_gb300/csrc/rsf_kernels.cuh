@@ -467,30 +467,47 @@ __global__ void __launch_bounds__(YB_TX) ypass_generic_kernel(const SubVolDev *_
 // each lane forms one local fit (f_out or f_in of one of the two columns) and
 // its e term; lanes 0 and 2 of the group write lambda (e_out - e_in).
 // ---------------------------------------------------------------------------
+// x column of lane f of a 4-lane group (column pair x, x+1): with the four
+// separate y fields lane f streams field f of both columns; with the pair
+// layout lane f streams pair f >> 1 of column x + (f & 1).
+template <bool PAIRS>
+__device__ __forceinline__ int zlane_col(int x, int f) {
+    return PAIRS ? x + (f & 1) : x + (f >> 1);
+}
+
+template <bool PAIRS>
 __device__ __forceinline__ void fits_and_data(const SubVolDev &s, const StepConst &c, int f, int x, int y, int o,
                                               bool live, float I, float2 B, const DebugOut &dbg, bool debug) {
-    // lane f: 0 -> f_out(x), 1 -> f_in(x), 2 -> f_out(x+1), 3 -> f_in(x+1);
-    // I is the image at that lane's voxel (prefetched by the caller).
-    const float bx_hi = __shfl_down_sync(0xffffffffu, B.x, 2);  // lanes 0,1 get IH(x), IHI(x)
-    const float by_lo = __shfl_up_sync(0xffffffffu, B.y, 2);    // lanes 2,3 get H(x+1), HI(x+1)
+    // Separate fields: B = (field f at x, field f at x+1); lane f forms
+    //   0 -> f_out(x), 1 -> f_in(x), 2 -> f_out(x+1), 3 -> f_in(x+1).
+    // Pair layout: B = (pair f>>1 at column x + (f&1)); lane f forms
+    //   0 -> f_out(x), 1 -> f_out(x+1), 2 -> f_in(x), 3 -> f_in(x+1).
+    // Both are num / den with num = lane f+2's B.x for f < 2, else B.y, and
+    // den = B.x for f < 2, else lane f-2's B.y.  I is the image at the
+    // lane's voxel (prefetched by the caller).
+    const float bx_hi = __shfl_down_sync(0xffffffffu, B.x, 2);
+    const float by_lo = __shfl_up_sync(0xffffffffu, B.y, 2);
     const float num = f < 2 ? bx_hi : B.y;
     const float den = f < 2 ? B.x : by_lo;
     const float fv = __fdiv_rn(num, den);
-    const int xc = x + (f >> 1);
+    const int xc = zlane_col<PAIRS>(x, f);
     const float d = __fsub_rn(I, fv);
     const float e = __fmul_rn(d, d);
-    const float e_in = __shfl_down_sync(0xffffffffu, e, 1);  // lanes 0, 2 get e_in of their column
-    if (live && (f & 1) == 0)
+    // the lane holding f_out of a column gets that column's e_in
+    const float e_in = __shfl_down_sync(0xffffffffu, e, PAIRS ? 2 : 1);
+    const bool outer = PAIRS ? f < 2 : (f & 1) == 0;
+    if (live && outer)
         s.db[((size_t)o * s.Hv + y) * s.Wp + xc] = data_factor(e, e_in, c.l1, c.l2, c.lam_equal != 0);
     if (debug && live) {
         const int r = c.r;
+        const int fin = outer ? 0 : 1;
         const size_t vi = ((size_t)(o + r) * s.H + (y + r)) * s.W + (xc + r);
-        dbg.f[(size_t)(f & 1) * dbg.n + vi] = fv;
-        dbg.f[(size_t)(2 + (f & 1)) * dbg.n + vi] = e;
+        dbg.f[(size_t)fin * dbg.n + vi] = fv;
+        dbg.f[(size_t)(2 + fin) * dbg.n + vi] = e;
     }
 }
 
-template <int K, bool DEBUG>
+template <int K, bool DEBUG, bool PAIRS = false>
 __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__restrict__ svs,
                                                              const int *__restrict__ pre, const StepConst c,
                                                              DebugOut dbg) {
@@ -504,13 +521,17 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
     const int f = threadIdx.x & 3;
     const int x = 2 * (tx * ZP_PAIRS + (threadIdx.x >> 2));
     const bool act = x < s.Wv;
-    const float *src = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)y * s.Wp + (act ? x : 0);
-    const size_t pstride = (size_t)s.Wp * s.Hv;
+    // separate fields: field f, column pair x; pair layout: pair f >> 1,
+    // column x + (f & 1), float2 elements (plane stride in floats doubles)
+    const float *src = PAIRS ? s.yb + (size_t)(f >> 1) * 2 * ((size_t)s.Wp * s.Hv * s.L) +
+                                   2 * ((size_t)y * s.Wp + (act ? x + (f & 1) : 0))
+                             : s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)y * s.Wp + (act ? x : 0);
+    const size_t pstride = (PAIRS ? 2 : 1) * (size_t)s.Wp * s.Hv;
     __shared__ float2 ring[RING * ZP_PAIRS * 4];
     __shared__ unsigned iring[RING * ZP_PAIRS * 4];
     // The image at this lane's voxel of output plane o (input plane o + r)
     // rides in the ring with element i = o + 2r.
-    const int xc = x + (f >> 1);
+    const int xc = zlane_col<PAIRS>(x, f);
     const bool live = act && xc < s.Wv;
     const size_t esz = c.img_f32 ? 4 : 1;
     const unsigned char *img0 = static_cast<const unsigned char *>(s.img) +
@@ -535,7 +556,7 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
                 if (c.img_f32) I = __uint_as_float(wd);
                 else I = (float)((wd >> (8 * ((shift0 + (unsigned)o * shift_step) & 3u))) & 0xffu);
             }
-            fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
         };
         stream_axis_c<K, RD>(rg, c, emit);
     } else {
@@ -553,7 +574,7 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
                 if (c.img_f32) I = __uint_as_float(wd);
                 else I = (float)((wd >> (8 * (unsigned)(reinterpret_cast<uintptr_t>(rg.sbyte(i)) & 3))) & 0xffu);
             }
-            fits_and_data(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
         };
         stream_axis<K>(rg, c, emit);
     }
@@ -782,7 +803,7 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
         const float out = update_phi(p0, dh, S.DT[C], kap, lap, c.dt, c.nu, c.mu);
         const size_t vi = (size_t)sc * k.WH + k.col;
         k.phi_out[vi] = out;
-        if (!isfinite(out)) atomicOr(flag, 1u);
+        if (!isfinite(out)) atomicOr(flag, kFlagNonFinite);
         if constexpr (DEBUG) {
             const bool inside = k.inside_xy && sc >= k.r && sc < k.L - k.r;
             if (!inside) {
@@ -857,7 +878,7 @@ __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepC
         const float dh = dirac<A>(p0, c.eps);
         const float out = update_phi(p0, dh, S.DT[C], kap, lap, c.dt, c.nu, c.mu);
         *op = out;
-        if (!isfinite(out)) atomicOr(flag, 1u);
+        if (!isfinite(out)) atomicOr(flag, kFlagNonFinite);
     }
     op += k.WH;
     S.P[C] = p3;

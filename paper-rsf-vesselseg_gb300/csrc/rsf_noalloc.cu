@@ -112,6 +112,7 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
 
     rsf::SubVolDev *d_table = reinterpret_cast<rsf::SubVolDev *>(base);
     int *d_pre = reinterpret_cast<int *>(base + 1024);
+    unsigned char *d_map = base + 2048;  // TMA map of the pair planes (fused path)
     unsigned *d_flag = reinterpret_cast<unsigned *>(base + kTableBytes);
     float *phi2 = reinterpret_cast<float *>(base + kTableBytes + kFlagBytes);
     float *xfields = reinterpret_cast<float *>(base + kTableBytes + kFlagBytes + kPhiBytes);
@@ -129,12 +130,11 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     d.xb = xfields;
     d.db = xfields;
     d.yb = yfields;
-    const int xb_w = rsf::choose_xb(&d.Wv, 1);
     const int whl[3] = {d.W, d.H, d.L};
-    const int zc = rsf::choose_zc(whl, 1);
     const int kspec = rsf::kernel_k(k, p->arith, false);
+    const rsf::LaunchShape sh = rsf::choose_shape(whl, 1, k, kspec);
     int tiles[rsf::NKERN];
-    rsf::tile_counts(d, kspec, xb_w, zc, tiles);
+    rsf::tile_counts(d, kspec, sh, tiles);
     int pre[2 * rsf::NKERN];  // per kernel: {0, tiles}
     for (int j = 0; j < rsf::NKERN; j++) {
         pre[2 * j] = 0;
@@ -159,13 +159,20 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     c.boundary = p->boundary;
     c.img_f32 = dtype == RSF_F32;
     c.nsv = 1;
-    c.xb_w = xb_w;
-    c.zc = zc;
+    c.xb_w = sh.xb_w;
+    c.xy_tx = sh.xy_tx;
+    c.zc = sh.zc;
+    alignas(64) unsigned char map[rsf::TMAP_BYTES];
+    if (sh.zt) {
+        if (!rsf::encode_pair_map(map, d)) return fail(RSF_ERR_CUDA, "rsf_evolve_noalloc: TMA tensor map encoding failed");
+        c.ymaps = d_map;
+    }
 
     // The table copies come from pageable host memory: they return once the
     // driver has staged the bytes, so the stack buffers may go out of scope.
     cudaError_t e = cudaMemcpyAsync(d_table, &d, sizeof d, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_pre, pre, sizeof pre, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && sh.zt) e = cudaMemcpyAsync(d_map, map, sizeof map, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(unsigned), st);
     for (int it = 0; it < iters && e == cudaSuccess; it++)
         e = rsf::launch_step(d_table, d_pre, tiles, c, it & 1, p->arith, d_flag, nullptr, st);

@@ -25,7 +25,14 @@ _PARAM_NAMES = ("lambda1", "lambda2", "mu", "nu")
 class _Evolve(torch.autograd.Function):
     @staticmethod
     def forward(ctx, phi0, image, lambda1, lambda2, mu, nu, params, iters, every, ws):
-        vals = {n: float(t) for n, t in zip(_PARAM_NAMES, (lambda1, lambda2, mu, nu))}
+        # The kernels take the parameters by value: host tensors are read
+        # without a device synchronisation, device tensors with one transfer
+        # for all four.
+        ts = [t.detach().reshape(()).to(torch.float64) for t in (lambda1, lambda2, mu, nu)]
+        if any(t.is_cuda for t in ts):
+            d = next(t.device for t in ts if t.is_cuda)
+            ts = torch.stack([t.to(d) for t in ts]).cpu().unbind()
+        vals = {n: float(t) for n, t in zip(_PARAM_NAMES, ts)}
         p = dataclasses.replace(params, **vals)
         phi = phi0.detach().to(torch.float32).contiguous().clone()
         ckpts = []
@@ -67,7 +74,9 @@ def evolve(phi0: torch.Tensor, image: torch.Tensor, params: Params, iters: int, 
            nu=None, checkpoint_every: int = 10, workspace: Workspace | None = None) -> torch.Tensor:
     """phi_T after `iters` steps, differentiable in phi0 and in any of
     lambda1, lambda2, mu, nu passed as tensors (others come from `params`).
-    phi0 and image are CUDA tensors (L, H, W); image uint8 or float32."""
+    phi0 and image are CUDA tensors (L, H, W); image uint8 or float32.
+    Parameter tensors on the host are read without synchronising the device;
+    CUDA parameter tensors cost one device-to-host transfer per call."""
     if iters < 1:
         raise ValueError("iters must be >= 1")
     if checkpoint_every < 1:
@@ -75,10 +84,11 @@ def evolve(phi0: torch.Tensor, image: torch.Tensor, params: Params, iters: int, 
     ws = workspace if workspace is not None else Workspace(phi0.numel())
     args = []
     for name, v in zip(_PARAM_NAMES, (lambda1, lambda2, mu, nu)):
+        # parameters that are not tensors become host scalars (no gradient)
         if v is None:
-            v = torch.tensor(float(getattr(params, name)), dtype=torch.float64, device=phi0.device)
+            v = torch.tensor(float(getattr(params, name)), dtype=torch.float64)
         elif not torch.is_tensor(v):
-            v = torch.tensor(float(v), dtype=torch.float64, device=phi0.device)
+            v = torch.tensor(float(v), dtype=torch.float64)
         args.append(v)
     return _Evolve.apply(phi0, image.contiguous(), *args, params, int(iters), int(checkpoint_every), ws)
 

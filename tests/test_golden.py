@@ -67,11 +67,17 @@ def test_heaviside_within_atan_tolerance(orc, gold, arith):
 
 @pytest.mark.parametrize("arith", [0, 1])
 def test_whole_iterations_track_reference(orc, gold, arith):
+    """Whole iterations against the reference's own: sign agreement >= 99.99 %
+    and max|dphi| <= 1e-4 max|phi|, except the portable arithmetic after
+    three iterations.  Its atan differs from CUDA's atanf by up to 1.2e-7 in
+    H, and the normalisation n = g/(|g| + 1e-6) amplifies that where phi is
+    flat: measured 3.2e-4 (sigma 1) and 2.3e-5 (sigma 3) of max|phi| after
+    three iterations, so that case is held to 1e-3."""
     phi0, I = gold["phi0"], gold["image"].astype(np.float32)
     p = orc.params(sigma=float(gold["sigma"]), eps=0.2, lambda1=1.0, mu=1.0, nu=65.025, dt=0.1, arith=arith)
     for iters, key in ((1, "phi1"), (3, "phi3")):
         got = orc.evolve(phi0, I, p, iters)
         want = gold[key]
-        assert float((np.sign(got) == np.sign(want)).mean()) >= 0.999
-        if iters == 1:
-            assert float(np.abs(got - want).max()) <= 1e-4 * float(np.abs(want).max())
+        assert float((np.sign(got) == np.sign(want)).mean()) >= 0.9999
+        bound = 1e-3 if (arith == 0 and iters == 3) else 1e-4
+        assert float(np.abs(got - want).max()) <= bound * float(np.abs(want).max())

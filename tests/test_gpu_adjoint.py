@@ -164,3 +164,127 @@ def test_adjoint_argument_errors(cuda, rsflib):
     with Workspace(999) as ws:
         with pytest.raises(RsfError):
             ws.step_adjoint(img, phi, u, _params())
+
+
+def _config4_volume(seed):
+    from rsf_gb300 import Params, synth
+
+    img, phi0, mask = synth.make_volume(synth.VolumeSpec((128, 128, 128), 12, 2.0, 6.0, seed))
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=0.001 * 255.0 ** 2, eps=1.0)
+    return img, phi0, mask, p
+
+
+def _fp64_vjp(step, x, img64, u, p, device):
+    names = ("lambda1", "lambda2", "mu", "nu")
+    xt = x.double().requires_grad_(True)
+    pr = [torch.tensor(f32(getattr(p, k)), dtype=torch.float64, device=device, requires_grad=True) for k in names]
+    (step(xt, img64, *pr) * u).sum().backward()
+    return xt.grad, np.array([v.grad.item() for v in pr])
+
+
+@pytest.mark.parametrize("seed", [40, 41])
+def test_config4_volume_step_adjoints_against_fp64_autograd(cuda, rsflib, orc, seed):
+    """Volumes of the differentiable workload at their stated size and inputs:
+    128^3 from the 128^3 generator (uint8 image 0-255, phi0 the +-3-clipped
+    signed distance), sigma 3, lambda1 = lambda2 = 1, mu 1, nu 0.001*255^2,
+    eps 1, dt 0.1.  The CUDA adjoint of one step at states 0, 10, 25 and 49
+    of the 50-step evolution, for a random upstream gradient, against the
+    float64 autograd restatement run on the GPU at the same FP32 state:
+    relative L2 error of dL/dphi and relative errors of the four parameter
+    gradients <= 1e-4."""
+    from oracle import rsf_autograd as ra
+    from rsf_gb300 import Workspace
+
+    img, phi0, mask, p = _config4_volume(seed)
+    ti = torch.from_numpy(img).to(cuda)
+    img64 = ti.double()
+    step = ra.Step(img.shape, orc.taps(p.sigma), f32(p.dt), f32(p.eps), 0, cuda)
+    gen = torch.Generator(device=cuda)
+    gen.manual_seed(seed)
+    with Workspace(img.size) as ws:
+        phi = torch.from_numpy(phi0).to(cuda)
+        for t in range(50):
+            if t in (0, 10, 25, 49):
+                u = torch.randn(phi.shape, device=cuda, generator=gen)
+                g = torch.zeros(4, dtype=torch.float64, device=cuda)
+                got = ws.step_adjoint(ti, phi, u, p, param_grads=g).double()
+                ws.check()
+                want, want_p = _fp64_vjp(step, phi, img64, u.double(), p, cuda)
+                rel = float(torch.linalg.vector_norm(got - want) / torch.linalg.vector_norm(want))
+                assert rel <= 1e-4, f"state {t}: dL/dphi relative L2 error {rel:.3g}"
+                gp = g.cpu().numpy()
+                for k in range(4):
+                    assert abs(gp[k] - want_p[k]) <= 1e-4 * max(abs(want_p[k]), 1e-3 * np.abs(want_p).max()), \
+                        (t, k, gp[k], want_p[k])
+            ws.evolve(ti, phi, p, 1)
+        ws.check()
+
+
+@pytest.mark.parametrize("seed", [40, 41])
+def test_config4_volume_chain_against_fp64_autograd(cuda, rsflib, orc, seed):
+    """The checkpointed chain on the same volumes, soft-Dice loss, against the
+    float64 vector-Jacobian products chained at the FP32 states of the CUDA
+    evolution (the trajectory the adjoint differentiates).
+
+    The horizon is 5 steps, not 50: where the clipped distance is flat
+    (g = 0), n = g/(|g| + 1e-6) has derivative 1e6, so each step multiplies
+    the gradient by up to ~1e5.  The float64 restatement measures
+    max|dL/dphi0| ~ 1e19 after 5 steps, ~1e46 after 10 and ~1e80 after 50
+    on a 64^3 volume of the same generator: beyond 5 steps the exact
+    gradient does not fit in FP32 (the adjoint then reports
+    RSF_ERR_NONFINITE), and finite differences do not converge.  Bars:
+    relative L2 error of dL/dphi0 and relative errors of the parameter
+    gradients <= 1e-3."""
+    from oracle import rsf_autograd as ra
+    from rsf_gb300 import Workspace, autograd
+
+    img, phi0, mask, p = _config4_volume(seed)
+    T = 5
+    names = ("lambda1", "lambda2", "mu", "nu")
+    ti = torch.from_numpy(img).to(cuda)
+    tm = torch.from_numpy(mask).to(cuda)
+    with Workspace(img.size) as ws:
+        prm = {k: torch.tensor(f32(getattr(p, k)), dtype=torch.float64, requires_grad=True) for k in names}
+        x = torch.from_numpy(phi0).to(cuda).requires_grad_(True)
+        out = autograd.evolve(x, ti, p, T, checkpoint_every=2, workspace=ws, **prm)
+        autograd.soft_dice_loss(out.double(), tm, p.eps).backward()
+        ws.check()
+        got = x.grad.double()
+        got_p = np.array([prm[k].grad.item() for k in names])
+        states = [torch.from_numpy(phi0).to(cuda)]
+        for _ in range(T):
+            nxt = states[-1].clone()
+            ws.evolve(ti, nxt, p, 1)
+            states.append(nxt)
+        ws.check()
+    assert torch.equal(states[-1], out.detach())
+    step = ra.Step(img.shape, orc.taps(p.sigma), f32(p.dt), f32(p.eps), 0, cuda)
+    img64 = ti.double()
+    xT = states[-1].double().requires_grad_(True)
+    autograd.soft_dice_loss(xT, tm, p.eps).backward()
+    u = xT.grad
+    want_p = np.zeros(4)
+    for t in reversed(range(T)):
+        u, gp = _fp64_vjp(step, states[t], img64, u, p, cuda)
+        want_p += gp
+    assert bool(torch.isfinite(got).all())
+    rel = float(torch.linalg.vector_norm(got - u) / torch.linalg.vector_norm(u))
+    assert rel <= 1e-3, f"dL/dphi0 relative L2 error {rel:.3g} (max|dL/dphi0| {float(u.abs().max()):.3g})"
+    for i, k in enumerate(names):
+        assert abs(got_p[i] - want_p[i]) <= 1e-3 * abs(want_p[i]), (k, got_p[i], want_p[i])
+
+
+def test_adjoint_reports_gradient_overflow(cuda, rsflib):
+    """An upstream gradient that overflows FP32 in the step's adjoint is
+    reported by the workspace check instead of passing silently."""
+    from rsf_gb300 import RsfError, Workspace
+
+    img, phi0, mask, p = _config4_volume(40)
+    ti = torch.from_numpy(img).to(cuda)
+    phi = torch.from_numpy(phi0).to(cuda)
+    u = torch.full(phi.shape, 3e38, device=cuda)
+    with Workspace(img.size) as ws:
+        ws.step_adjoint(ti, phi, u, p)
+        with pytest.raises(RsfError, match="overflowed"):
+            ws.check()
+        ws.check()  # the flag is cleared once reported
