@@ -398,7 +398,7 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
     c.xb_w = sh.xb_w;
-    c.xy_tx = sh.xy_tx;
+    c.pairs = sh.pairs;
     c.zc = sh.zc;
     c.ymaps = sh.zt ? maps : nullptr;
     c.box = (int)p->sigma2;

@@ -9,7 +9,7 @@ constexpr int MAXK = 128;  // largest supported tap count (sigma up to ~18)
 
 // Kernel tilings (the launchers derive tile counts from them).
 constexpr int XP_ROWS = 4;     // x-pass: rows per block (one warp per row)
-constexpr int YP_PAIRS = 128;  // y-pass: column pairs per block (one thread each)
+constexpr int YP_COLS = 128;   // y-pass: columns per block (one column of one pair per thread)
 constexpr int YB_TX = 128;     // generic y-pass: columns per block
 constexpr int YB_YB = 16;      // generic y-pass: outputs per thread along y
 constexpr int ZP_PAIRS = 32;   // z-pass: column pairs per block (four lanes each)
@@ -23,17 +23,13 @@ constexpr int ST_ZC = 64;      // stencil: planes per block (32 when that gives 
 // The x-pass lane width (outputs per lane) is chosen per launch from these.
 constexpr int XB_CHOICES[2] = {5, 9};
 
-// Fused x/y-pass (rsf_xy.cuh): rows per chunk, which must divide the tap
-// count, and the range of its tile width TX (a multiple of XY_R, chosen per
-// launch; the block has 2 TX threads).
-constexpr int XY_R = 7;
-constexpr int XY_TX_MIN = 84;
-constexpr int XY_TX_MAX = 154;
 
 // One sub-volume as the kernels see it.
-//   xb: 4 x-pass fields, each Wp x H x L   (row stride Wp)
-//   yb: 4 y-pass fields, each Wp x Hv x L; after the fused x/y-pass two
-//       float2 pair planes (H, 1-H) and (I H, I (1-H)), each Wp x Hv x L
+//   xb: x-pass fields, each Wp x H x L   (row stride Wp)
+//   yb: y-pass fields, each Wp x Hv x L
+//   The specialised tap counts keep the fields as two float2 pair planes,
+//   pair 0 (H, 1-H) and pair 1 (I H, I (1-H)); the run-time-k kernels as four
+//   separate float planes (H, 1-H, I H, I (1-H)).
 //   db: data factor lambda (e_out - e_in) of the valid region, Wp x Hv x Lv;
 //       it reuses the x-pass storage, which is dead once the y-pass has run.
 //       With the box e-term it holds f_out and f_in of the valid region
@@ -62,10 +58,10 @@ struct StepConst {
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
     int xb_w;       // x-pass outputs per lane for this launch
-    int xy_tx;      // fused x/y-pass tile width for this launch (0: separate passes)
+    int pairs;      // 1: x/y fields in float2 pair planes (specialised tap counts)
     int zc;         // stencil planes per block for this launch
     int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
-    const void *ymaps;  // fused path: per sub-volume TMA map of the pair planes (TMAP_BYTES each)
+    const void *ymaps;  // per sub-volume TMA map of the y-pass pair planes (TMAP_BYTES each), or null
 };
 
 // TMA tensor maps (CUtensorMap) as the kernels see them: 128 bytes each, in
@@ -75,6 +71,7 @@ constexpr int TMAP_BYTES = 128;
 // when the driver's encoder is unavailable or refuses the layout.
 bool encode_pair_map(void *out, const SubVolDev &d);
 bool tensor_maps_available();
+bool tma_z_requested();
 
 // Optional per-voxel debug outputs (8 fields, full-volume layout).
 struct DebugOut {
@@ -82,7 +79,7 @@ struct DebugOut {
     int64_t n;
 };
 
-constexpr int NKERN = 4;  // x-pass (or fused x/y-pass), y-pass, z-pass, stencil
+constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil
 
 // Bits of the per-workspace error flag the kernels set.
 constexpr unsigned kFlagNonFinite = 1u;  // a non-finite value was written to phi
@@ -96,15 +93,16 @@ inline bool is_specialised(int k) { return k == 21 || k == 29 || k == 35; }
 inline int kernel_k(int k, int arith, bool debug, int box = 0) {
     return (is_specialised(k) && arith == 0 && !debug && box == 0) ? k : 0;
 }
-// Specialised tap counts whose x and y correlations run fused (XY_R | k).
-inline bool fused_xy(int kspec) { return kspec == 21 || kspec == 35; }
+// Specialised tap counts whose z-pass can run fed by TMA (its image prefetch
+// ring depth divides k).
+inline bool tma_z(int kspec) { return kspec == 21 || kspec == 35; }
 constexpr int MAX_BOX = 8;  // largest e-term box radius
 
 // Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
 // Per-launch tile shapes of a batch.
 struct LaunchShape {
     int xb_w;   // x-pass outputs per lane (separate passes)
-    int xy_tx;  // fused x/y-pass tile width (0: separate passes)
+    int pairs;  // 1: x/y fields in float2 pair planes (specialised tap counts)
     int zt;     // 1: the fused path's z-pass loads planes with TMA (needs a map per sub-volume)
     int zc;     // stencil planes per block
 };
@@ -112,7 +110,6 @@ struct LaunchShape {
 LaunchShape choose_shape(const int *whl, int n, int k, int kspec);
 void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NKERN]);
 int choose_xb(const int *Wv, int n);
-int choose_xy_tx(const int *whl, int n, int k);
 int choose_zc(const int *whl, int n);  // whl: W, H, L of each sub-volume
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
 
@@ -143,10 +140,8 @@ RSF_DECLARE_K(21)
 RSF_DECLARE_K(29)
 RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
-cudaError_t launch_xypass_21(const SubVolDev *, const int *, int, const StepConst &, int parity, cudaStream_t);
-cudaError_t launch_xypass_35(const SubVolDev *, const int *, int, const StepConst &, int parity, cudaStream_t);
-cudaError_t config_xypass_21();
-cudaError_t config_xypass_35();
+cudaError_t config_ztpass_21();
+cudaError_t config_ztpass_35();
 cudaError_t launch_ztpass_21(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
 cudaError_t launch_ztpass_35(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,

@@ -183,28 +183,51 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
     float *st23 = reinterpret_cast<float *>(in);
     const float2 *src = reinterpret_cast<const float2 *>(in + XB * lane);
     float2 acc[XB];
-    xconv_pair<K, XB>(src, c, taps_s, k, acc);
+    if constexpr (K > 0) {
+        // two float2 pair planes: each pair's results are staged as float2
+        // and written as float4 (two columns)
+        float2 *s01 = reinterpret_cast<float2 *>(st01), *s23 = reinterpret_cast<float2 *>(st23);
+        xconv_pair<K, XB>(src, c, taps_s, k, acc);
 #pragma unroll
-    for (int m = 0; m < XB; ++m) {
-        st01[XB * lane + m] = acc[m].x;
-        st01[XT + XB * lane + m] = acc[m].y;
-    }
-    xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
-    __syncwarp();
+        for (int m = 0; m < XB; ++m) s01[XB * lane + m] = acc[m];
+        xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
+        __syncwarp();
 #pragma unroll
-    for (int m = 0; m < XB; ++m) {
-        st23[XB * lane + m] = acc[m].x;
-        st23[XT + XB * lane + m] = acc[m].y;
-    }
-    __syncwarp();
-    const size_t fstride = (size_t)s.Wp * s.H * s.L;
-    const size_t orow = ((size_t)z * s.H + y) * s.Wp;
+        for (int m = 0; m < XB; ++m) s23[XB * lane + m] = acc[m];
+        __syncwarp();
+        const size_t pstride = (size_t)s.Wp * s.H * s.L;
+        const size_t orow = ((size_t)z * s.H + y) * s.Wp;
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        const float4 *sf = reinterpret_cast<const float4 *>((f < 2 ? st01 : st23) + (f & 1) * XT);
-        float4 *dst = reinterpret_cast<float4 *>(s.xb + f * fstride + orow + x0);
-        for (int e = lane; e < XT / 4; e += 32)
-            if (x0 + 4 * e < s.Wv) dst[e] = sf[e];
+        for (int pp = 0; pp < 2; ++pp) {
+            const float4 *sf = reinterpret_cast<const float4 *>(pp ? s23 : s01);
+            float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(s.xb) + pp * pstride + orow + x0);
+            for (int e = lane; e < XT / 2; e += 32)
+                if (x0 + 2 * e < s.Wv) dst[e] = sf[e];
+        }
+    } else {
+        xconv_pair<K, XB>(src, c, taps_s, k, acc);
+#pragma unroll
+        for (int m = 0; m < XB; ++m) {
+            st01[XB * lane + m] = acc[m].x;
+            st01[XT + XB * lane + m] = acc[m].y;
+        }
+        xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < XB; ++m) {
+            st23[XB * lane + m] = acc[m].x;
+            st23[XT + XB * lane + m] = acc[m].y;
+        }
+        __syncwarp();
+        const size_t fstride = (size_t)s.Wp * s.H * s.L;
+        const size_t orow = ((size_t)z * s.H + y) * s.Wp;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const float4 *sf = reinterpret_cast<const float4 *>((f < 2 ? st01 : st23) + (f & 1) * XT);
+            float4 *dst = reinterpret_cast<float4 *>(s.xb + f * fstride + orow + x0);
+            for (int e = lane; e < XT / 4; e += 32)
+                if (x0 + 4 * e < s.Wv) dst[e] = sf[e];
+        }
     }
 }
 
@@ -405,30 +428,31 @@ __device__ __forceinline__ void conv_block_rt(const float *__restrict__ base, si
 }
 
 // ---------------------------------------------------------------------------
-// y-pass.  One thread streams a column pair of one field of one z plane.
+// y-pass.  One thread streams one column of one pair plane of one z plane
+// (float2 elements: both fields of the pair, one packed multiply-add).
 // ---------------------------------------------------------------------------
 template <int K>
-__global__ void __launch_bounds__(YP_PAIRS) ypass_kernel(const SubVolDev *__restrict__ svs,
-                                                         const int *__restrict__ pre, const StepConst c) {
+__global__ void __launch_bounds__(YP_COLS) ypass_kernel(const SubVolDev *__restrict__ svs,
+                                                        const int *__restrict__ pre, const StepConst c) {
     const int b = blockIdx.x;
     const int sv = find_sv(pre, c.nsv, b);
     const SubVolDev s = svs[sv];
     int t = b - __ldg(pre + sv);
-    const int ntx = (s.Wv + 2 * YP_PAIRS - 1) / (2 * YP_PAIRS);
+    const int ntx = (s.Wv + YP_COLS - 1) / YP_COLS;
     const int tx = t % ntx;
     t /= ntx;
-    const int f = t & 3;
-    const int z = t >> 2;
-    __shared__ float2 ring[RING * YP_PAIRS];
-    const int x = 2 * (tx * YP_PAIRS + threadIdx.x);
+    const int p = t & 1;
+    const int z = t >> 1;
+    __shared__ float2 ring[RING * YP_COLS];
+    const int x = tx * YP_COLS + threadIdx.x;
     if (x >= s.Wv) return;
-    const float *src = s.xb + f * ((size_t)s.Wp * s.H * s.L) + (size_t)z * s.H * s.Wp + x;
-    float *dst = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)z * s.Hv * s.Wp + x;
+    const float *src = s.xb + 2 * ((size_t)p * s.Wp * s.H * s.L + (size_t)z * s.H * s.Wp + x);
+    float2 *dst = reinterpret_cast<float2 *>(s.yb) + (size_t)p * s.Wp * s.Hv * s.L + (size_t)z * s.Hv * s.Wp + x;
     const size_t wp = (size_t)s.Wp;
     // The y-pass is bound by HBM bandwidth: it keeps the deeper 8-slot ring
     // (more loads in flight) rather than the compile-time-slot ring.
-    auto emit = [&](int o, float2 v, int) { *reinterpret_cast<float2 *>(dst + (size_t)o * wp) = v; };
-    const Ring rg = {ring + threadIdx.x, YP_PAIRS, src, wp, s.H, true};
+    auto emit = [&](int o, float2 v, int) { dst[(size_t)o * wp] = v; };
+    const Ring rg = {ring + threadIdx.x, YP_COLS, src, 2 * wp, s.H, true};
     stream_axis<K>(rg, c, emit);
 }
 

@@ -112,7 +112,7 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
 
     rsf::SubVolDev *d_table = reinterpret_cast<rsf::SubVolDev *>(base);
     int *d_pre = reinterpret_cast<int *>(base + 1024);
-    unsigned char *d_map = base + 2048;  // TMA map of the pair planes (fused path)
+    unsigned char *d_map = base + 2048;  // TMA map of the y-pass pair planes
     unsigned *d_flag = reinterpret_cast<unsigned *>(base + kTableBytes);
     float *phi2 = reinterpret_cast<float *>(base + kTableBytes + kFlagBytes);
     float *xfields = reinterpret_cast<float *>(base + kTableBytes + kFlagBytes + kPhiBytes);
@@ -160,7 +160,7 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     c.img_f32 = dtype == RSF_F32;
     c.nsv = 1;
     c.xb_w = sh.xb_w;
-    c.xy_tx = sh.xy_tx;
+    c.pairs = sh.pairs;
     c.zc = sh.zc;
     alignas(64) unsigned char map[rsf::TMAP_BYTES];
     if (sh.zt) {

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -65,30 +67,6 @@ int choose_zc(const int *whl, int n) {
     return blocks >= 4LL * 2 * sm_count() ? ST_ZC : ST_ZC / 2;
 }
 
-// Fused x/y-pass tile width: the multiple of XY_R in [XY_TX_MIN, XY_TX_MAX]
-// with the least estimated work over the batch.  A tile of TX outputs along x
-// forms the fields of TX + k - 1 inputs (about 50 instructions each) and
-// correlates TX columns along x and y (about 2 x 2 (k + 1) each), for all H
-// rows of all L planes.
-int choose_xy_tx(const int *whl, int n, int k) {
-    int best = XY_TX_MAX;
-    double best_cost = -1.0;
-    for (int tx = XY_TX_MAX; tx >= XY_TX_MIN; tx -= XY_R) {
-        double cost = 0.0;
-        for (int i = 0; i < n; i++) {
-            const int Wv = whl[3 * i] - k + 1, Hv = whl[3 * i + 1] - k + 1, Lv = whl[3 * i + 2] - k + 1;
-            if (Wv <= 0 || Hv <= 0 || Lv <= 0) continue;
-            const double tiles = (double)((Wv + tx - 1) / tx) * whl[3 * i + 1] * whl[3 * i + 2];
-            cost += tiles * (50.0 * (tx + k - 1) + 4.0 * (k + 1) * tx);
-        }
-        if (best_cost < 0.0 || cost < best_cost) {
-            best_cost = cost;
-            best = tx;
-        }
-    }
-    return best;
-}
-
 LaunchShape choose_shape(const int *whl, int n, int k, int kspec) {
     LaunchShape sh;
     std::vector<int> wv((size_t)n);
@@ -98,8 +76,8 @@ LaunchShape choose_shape(const int *whl, int n, int k, int kspec) {
         wv[(size_t)i] = Wv;
     }
     sh.xb_w = choose_xb(wv.data(), n);
-    sh.xy_tx = fused_xy(kspec) ? choose_xy_tx(whl, n, k) : 0;
-    sh.zt = fused_xy(kspec) && tensor_maps_available() ? 1 : 0;
+    sh.pairs = kspec > 0 ? 1 : 0;
+    sh.zt = tma_z(kspec) && tma_z_requested() && tensor_maps_available() ? 1 : 0;
     sh.zc = choose_zc(whl, n);
     return sh;
 }
@@ -124,11 +102,19 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 }  // namespace
 
-// The pair planes as a 4-D float tensor (2 Wp floats, Hv rows, L planes, 2
+// The y-pass pair planes as a 4-D float tensor (2 Wp floats, Hv rows, L planes, 2
 // pairs); the z-pass box is one plane of a ZT_X x ZT_Y column tile of both
 // pairs.  Rows are 8 Wp bytes, a multiple of 32, and the pool offsets keep
 // every base 64-byte aligned, as TMA requires.
 bool tensor_maps_available() { return tensor_map_encoder() != nullptr; }
+
+// The TMA-fed z-pass runs when the environment variable RSF_ZPASS is "tma"
+// (read at each call); the default is the streaming z-pass, which measured
+// faster on the 48-sub-volume batch (6.81 against 7.58 ms per launch).
+bool tma_z_requested() {
+    const char *v = std::getenv("RSF_ZPASS");
+    return v && std::strcmp(v, "tma") == 0;
+}
 
 bool encode_pair_map(void *out, const SubVolDev &d) {
     static_assert(sizeof(CUtensorMap) == TMAP_BYTES, "tensor map size");
@@ -147,12 +133,10 @@ bool encode_pair_map(void *out, const SubVolDev &d) {
 void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NKERN]) {
     const bool valid = d.Wv > 0;
     const int xt = 32 * sh.xb_w, zc = sh.zc;
-    if (!valid) tiles[0] = 0;
-    else if (fused_xy(kspec)) tiles[0] = ((d.Wv + sh.xy_tx - 1) / sh.xy_tx) * d.L;
-    else tiles[0] = ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L;
-    if (!valid || fused_xy(kspec)) tiles[1] = 0;
+    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L : 0;
+    if (!valid) tiles[1] = 0;
     else if (kspec == 0) tiles[1] = ((d.Wv + YB_TX - 1) / YB_TX) * ((d.Hv + YB_YB - 1) / YB_YB) * 4 * d.L;
-    else tiles[1] = ((d.Wv + 2 * YP_PAIRS - 1) / (2 * YP_PAIRS)) * 4 * d.L;
+    else tiles[1] = ((d.Wv + YP_COLS - 1) / YP_COLS) * 2 * d.L;  // one column of one pair per thread
     if (!valid) tiles[2] = 0;
     else if (sh.zt) tiles[2] = ((d.Wv + ZT_X - 1) / ZT_X) * ((d.Hv + ZT_Y - 1) / ZT_Y);
     else if (kspec == 0) tiles[2] = ((d.Wv + ZB_TX - 1) / ZB_TX) * ((d.Lv + ZB_ZB - 1) / ZB_ZB) * d.Hv;
@@ -167,8 +151,8 @@ cudaError_t configure_device() {
     if (e == cudaSuccess) e = config_xpass_21();
     if (e == cudaSuccess) e = config_xpass_29();
     if (e == cudaSuccess) e = config_xpass_35();
-    if (e == cudaSuccess) e = config_xypass_21();
-    if (e == cudaSuccess) e = config_xypass_35();
+    if (e == cudaSuccess) e = config_ztpass_21();
+    if (e == cudaSuccess) e = config_ztpass_35();
     return e;
 }
 
@@ -185,11 +169,7 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
     const unsigned rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto mark = [&](int i) { return ev ? cudaEventRecordWithFlags(ev[i], st, rec_flags) : cudaSuccess; };
     if ((e = mark(0)) != cudaSuccess) return e;
-    if (tot[0] > 0 && fused_xy(kspec)) {
-        e = kspec == 21 ? launch_xypass_21(svs, pre, tot[0], c, parity, st)
-                        : launch_xypass_35(svs, pre, tot[0], c, parity, st);
-        if (e != cudaSuccess) return e;
-    } else if (tot[0] > 0) {
+    if (tot[0] > 0) {
         switch (kspec) {
             case 21: e = launch_xpass_21(svs, pre, tot[0], c, parity, arith, st); break;
             case 29: e = launch_xpass_29(svs, pre, tot[0], c, parity, arith, st); break;
@@ -209,7 +189,7 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
         if (e != cudaSuccess) return e;
     }
     if ((e = mark(2)) != cudaSuccess) return e;
-    if (tot[2] > 0 && fused_xy(kspec) && c.ymaps) {
+    if (tot[2] > 0 && tma_z(kspec) && c.ymaps) {
         e = kspec == 21 ? launch_ztpass_21(svs, pre + 2 * n1, tot[2], c, flag, st)
                         : launch_ztpass_35(svs, pre + 2 * n1, tot[2], c, flag, st);
         if (e != cudaSuccess) return e;

@@ -13,7 +13,7 @@ namespace rsf {
 cudaError_t RSF_CAT(launch_ypass_, RSF_K)(const SubVolDev *svs, const int *pre, int blocks, const StepConst &c,
                                           cudaStream_t st) {
 #if RSF_K > 0
-    ypass_kernel<RSF_K><<<blocks, YP_PAIRS, 0, st>>>(svs, pre, c);
+    ypass_kernel<RSF_K><<<blocks, YP_COLS, 0, st>>>(svs, pre, c);
 #else
     ypass_generic_kernel<0><<<blocks, YB_TX, 0, st>>>(svs, pre, c);
 #endif

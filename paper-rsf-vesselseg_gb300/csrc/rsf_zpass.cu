@@ -16,7 +16,7 @@ cudaError_t RSF_CAT(launch_zpass_, RSF_K)(const SubVolDev *svs, const int *pre, 
     const DebugOut none = {nullptr, 0};
 #if RSF_K > 0
     (void)dbg;
-    if (c.xy_tx > 0) zpass_kernel<RSF_K, false, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
+    if (c.pairs) zpass_kernel<RSF_K, false, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
     else zpass_kernel<RSF_K, false, false><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
 #else
     if (dbg) zpass_generic_kernel<true><<<blocks, ZB_TX, 0, st>>>(svs, pre, c, *dbg);

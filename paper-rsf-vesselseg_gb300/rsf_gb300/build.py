@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"
 # once per tap specialisation so that the objects build in parallel.
 CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in ("xpass", "ypass", "zpass")
              for k in (0, 21, 29, 35)]
-            + [(f"rsf_xypass.cu", f"rsf_xypass_k{k}", [f"-DRSF_K={k}"]) for k in (21, 35)]
+            + [("rsf_ztpass.cu", f"rsf_ztpass_k{k}", [f"-DRSF_K={k}"]) for k in (21, 35)]
             + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
                ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", []),
                ("rsf_sdf.cu", "rsf_sdf", []), ("rsf_adjoint.cu", "rsf_adjoint", []),

@@ -265,3 +265,30 @@ def test_evolve_host_pinned_and_pageable_agree(orc, ws_big, cuda):
     ws_big.evolve_host_ptr(ti.data_ptr(), "uint8", tp.data_ptr(), phi0.shape, p, 3)
     want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), 3)
     assert _bits_equal(a, want) and _bits_equal(tp.numpy(), want)
+
+
+@pytest.mark.parametrize("sigma", [3.0, 5.0])
+def test_tma_z_pass_bit_exact(sigma, orc, ws_big, cuda, monkeypatch):
+    """The z-pass fed by TMA tile loads (selected with RSF_ZPASS=tma, 21 and
+    35 taps) against the oracle and against the default streaming z-pass, on
+    a batch with a thin and an all-border sub-volume and on an image of
+    float32."""
+    import torch
+    from rsf_gb300 import Params
+
+    shapes = [(40, 44, 48), (30, 33, 70), (9, 9, 9), (64, 38, 52)]
+    p = Params(sigma=sigma, dt=0.1, mu=1.0, lambda1=1.0, lambda2=0.5, nu=65.025, eps=1.0)
+    for dtype in ("u8", "f32"):
+        inputs = [_inputs(s, seed=30 + i, dtype=dtype)[:2] for i, s in enumerate(shapes)]
+        outs = {}
+        for mode in ("tma", "stream"):
+            monkeypatch.setenv("RSF_ZPASS", mode)
+            pairs = [(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda)) for img, phi0 in inputs]
+            ws_big.evolve_batched(pairs, p, 3)
+            ws_big.check()
+            outs[mode] = [b.cpu().numpy() for _, b in pairs]
+        monkeypatch.delenv("RSF_ZPASS")
+        for (img, phi0), a, b in zip(inputs, outs["tma"], outs["stream"]):
+            assert _bits_equal(a, b), f"{img.shape} {dtype}: TMA and streaming z-pass differ"
+            want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), 3)
+            assert _bits_equal(a, want), f"{img.shape} {dtype}: {_diff_report(a, want)}"
