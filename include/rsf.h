@@ -67,6 +67,20 @@ typedef enum {
     RSF_ARITH_REFERENCE = 1
 } rsf_arith;
 
+typedef enum {
+    /* the reference's data term (kernel.cu:25-55): e = (I - f)^2 at the voxel,
+     * or its box sum with sigma2 >= 1 */
+    RSF_DATA_TERM_REFERENCE = 0,
+    /* the region-scalable fitting energy's data term written out, with no
+     * counterpart in the reference: e = I^2 K*1 - 2 I K*f + K*f^2 on the valid
+     * region of the blur (K the same valid Gaussian correlation as the fits,
+     * f the fit field, 1 in the border band); the border band keeps
+     * (I - 1)^2.  Run-time-k kernels; needs sigma2 < 1; no adjoint.  On
+     * first use the workspace allocates 16 more bytes per voxel of its
+     * capacity for the blurred fields. */
+    RSF_DATA_TERM_GAUSSIAN = 1
+} rsf_data_term;
+
 /* Parameters of one evolution.  Defaults (rsf_params_default) are the
  * reference's command-line defaults, main.cpp:91-97. */
 typedef struct {
@@ -80,7 +94,8 @@ typedef struct {
     float sigma2;   /* --sigma2 0.0: (int) radius of the e-term box window, 0..8 */
     int32_t boundary; /* rsf_boundary */
     int32_t arith;    /* rsf_arith */
-    int32_t reserved[6];
+    int32_t data_term; /* rsf_data_term */
+    int32_t reserved[5];
 } rsf_params;
 
 /* One sub-volume of a batch.  All pointers are device pointers. */

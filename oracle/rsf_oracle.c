@@ -26,6 +26,8 @@
  *   CUDA_RSF/main.cpp:174-183   phi0 = sdf(seed - 13): this project's own
  *                               definition (tiralib's sdf is not in the
  *                               reference), see oracle_signed_distance
+ * and one mode of this project's own with no counterpart in the reference:
+ * the expanded Gaussian data term (data_term = 1, gaussian_data_terms).
  *
  * Arithmetic follows the reference kernels operation by operation.  Every
  * a*b+c that nvcc contracts into a fused multiply-add under its default
@@ -73,7 +75,7 @@ typedef struct {
     int32_t boundary;  /* 0: reference x=0 rule (previous row), 1: clamp */
     int32_t mag_form;  /* contraction order of |g|^2, see grad_mag2() */
     int32_t arith;     /* 0 portable float sequences, 1 reference double spots */
-    int32_t reserved;
+    int32_t data_term; /* 0 the reference's (I - f)^2 / box form, 1 expanded Gaussian */
 } oracle_params;
 
 static inline size_t idx3(int64_t x, int64_t y, int64_t z, int64_t W, int64_t H) {
@@ -379,6 +381,60 @@ static void data_terms(const float *I, const float *fo, const float *fi, float *
 }
 
 /*
+ * The expanded Gaussian data term (data_term = 1; no counterpart in the
+ * reference, whose kernel.cu:25-55 takes (I - f)^2 at the voxel).  It is the
+ * region-scalable fitting energy's data term written out:
+ *   e_i(c) = I(c)^2 (K*1)(c) - 2 I(c) (K*f_i)(c) + (K*f_i^2)(c)
+ * on the valid region of the blur, where K is the same valid separable
+ * correlation as the local fits (x, then y, then z, taps ascending, fused
+ * multiply-adds from +0) and f_i the full-volume fit field (1 in the border
+ * band).  K*1 is the same constant s3 at every valid voxel.  FP32 sequence:
+ *   b = fmaf(I*I, s3, K*f^2);  e = fmaf(-2*I, K*f, b).
+ * The border band keeps the reference form (I - 1)^2.
+ */
+static float ones_correlation(const float *g, int k) {
+    float sx = 0.0f, sy = 0.0f, s3 = 0.0f;
+    for (int t = 0; t < k; t++) sx = fmaf(1.0f, g[t], sx);
+    for (int t = 0; t < k; t++) sy = fmaf(sx, g[t], sy);
+    for (int t = 0; t < k; t++) s3 = fmaf(sy, g[t], s3);
+    return s3;
+}
+
+static int gaussian_data_terms(const float *I, const float *fo, const float *fi, float *eo, float *ei,
+                               int64_t W, int64_t H, int64_t L, const float *g, int k) {
+    data_terms(I, fo, fi, eo, ei, W, H, L, 0);  /* the border band's form everywhere first */
+    int64_t r = (k - 1) / 2, Wo = W - k + 1, Ho = H - k + 1, Lo = L - k + 1;
+    if (Wo <= 0 || Ho <= 0 || Lo <= 0) return 0;
+    size_t n = (size_t)W * H * L, nv = (size_t)Wo * Ho * Lo;
+    float *fld = (float *)malloc(sizeof(float) * n);
+    float *bx = (float *)malloc(sizeof(float) * (size_t)Wo * H * L);
+    float *by = (float *)malloc(sizeof(float) * (size_t)Wo * Ho * L);
+    float *kb = (float *)malloc(sizeof(float) * nv * 4);
+    if (!fld || !bx || !by || !kb) { free(fld); free(bx); free(by); free(kb); return -1; }
+    const float *src[2] = {fo, fi};
+    for (int j = 0; j < 4; j++) {
+        const float *f = src[j >> 1];
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)n; i++) fld[i] = (j & 1) ? f[i] * f[i] : f[i];
+        conv_x(fld, bx, W, H, L, g, k);
+        conv_y(bx, by, Wo, H, L, g, k);
+        conv_z(by, kb + (size_t)j * nv, Wo, Ho, L, g, k);
+    }
+    const float s3 = ones_correlation(g, k);
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < Lo; z++)
+        for (int64_t y = 0; y < Ho; y++)
+            for (int64_t x = 0; x < Wo; x++) {
+                size_t v = idx3(x, y, z, Wo, Ho), c = idx3(x + r, y + r, z + r, W, H);
+                float Ic = I[c], a = Ic * Ic, m2 = -2.0f * Ic;
+                eo[c] = fmaf(m2, kb[v], fmaf(a, s3, kb[nv + v]));
+                ei[c] = fmaf(m2, kb[2 * nv + v], fmaf(a, s3, kb[3 * nv + v]));
+            }
+    free(fld); free(bx); free(by); free(kb);
+    return 0;
+}
+
+/*
  * Final_phi, kernel.cu:384, with nvcc's contraction:
  *   phi - (dh*(e*(Eo-Ei)))*dt + ((v*dt)*dh)*nd + meu*(dt*(div-nd))
  *   = fma(meu, dt*(div-nd), fma((v*dt)*dh, nd, fma(-(dh*(e*(Eo-Ei))), dt, phi)))
@@ -457,7 +513,11 @@ int oracle_step_f32(const float *phi, const float *I, float *phi_out,
         F[F_FI][i] = F[F_BII][i] / F[F_BHI][i];
     }
     /* adddevice: main.cpp:293 */
-    data_terms(I, F[F_FO], F[F_FI], F[F_EO], F[F_EI], W, H, L, (int)p->sigma2);
+    if (p->data_term == 1) {
+        if (gaussian_data_terms(I, F[F_FO], F[F_FI], F[F_EO], F[F_EI], W, H, L, g, k)) { free(buf); return -1; }
+    } else {
+        data_terms(I, F[F_FO], F[F_FI], F[F_EO], F[F_EI], W, H, L, (int)p->sigma2);
+    }
     /* deri_heaviside_cal, Final_PHI_cal: main.cpp:296-300 */
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)n; i++) {
@@ -616,6 +676,28 @@ int oracle_step_f64(const double *phi, const float *I, double *phi_out,
     if (rc) { free(buf); return -1; }
     int s = (int)p->sigma2;
     double w = 1.0 / (double)((2 * s + 1) * (2 * s + 1));
+    /* expanded Gaussian data term (data_term = 1): the blurs K*f, K*f^2 in
+     * double, e = I^2 K*1 - 2 I K*f + K*f^2 on the valid region */
+    double *kb = NULL, s3 = 0.0;
+    int64_t r = (k - 1) / 2, Wo = W - k + 1, Ho = H - k + 1, Lo = L - k + 1;
+    int gauss = p->data_term == 1 && Wo > 0 && Ho > 0 && Lo > 0;
+    if (gauss) {
+        double *fld = (double *)malloc(sizeof(double) * n);
+        kb = (double *)malloc(sizeof(double) * n * 4);
+        if (!fld || !kb) { free(fld); free(kb); free(buf); return -1; }
+        for (int j = 0; j < 4; j++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < (int64_t)n; i++) {
+                double f = (j < 2) ? F[D_BIO][i] / F[D_BHO][i] : F[D_BII][i] / F[D_BHI][i];
+                fld[i] = (j & 1) ? f * f : f;
+            }
+            if (blur_padded_d(fld, kb + (size_t)j * n, W, H, L, g, k)) { free(fld); free(kb); free(buf); return -1; }
+        }
+        free(fld);
+        double sx = 0.0;
+        for (int t = 0; t < k; t++) sx += g[t];
+        s3 = sx * sx * sx;
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t z = 0; z < L; z++)
         for (int64_t y = 0; y < H; y++)
@@ -624,7 +706,12 @@ int oracle_step_f64(const double *phi, const float *I, double *phi_out,
                 double fo = F[D_BIO][c] / F[D_BHO][c];
                 double fi = F[D_BII][c] / F[D_BHI][c];
                 double eo = 0.0, ei = 0.0;
-                for (int u = -s; u <= s; u++)
+                int inside = gauss && x >= r && x < Wo + r && y >= r && y < Ho + r && z >= r && z < Lo + r;
+                if (inside) {
+                    double Ic = I[c];
+                    eo = Ic * Ic * s3 - 2.0 * Ic * kb[c] + kb[n + c];
+                    ei = Ic * Ic * s3 - 2.0 * Ic * kb[2 * n + c] + kb[3 * n + c];
+                } else for (int u = -s; u <= s; u++)
                     for (int v = -s; v <= s; v++)
                         for (int q = -s; q <= s; q++) {
                             int64_t yy = y + u, xx = x + v, zz = z + q;
@@ -639,6 +726,7 @@ int oracle_step_f64(const double *phi, const float *I, double *phi_out,
                 phi_out[c] = ph - dh * data * p->dt + (double)p->nu * p->dt * dh * F[D_KAP][c]
                              + (double)p->mu * p->dt * (F[D_LAP][c] - F[D_KAP][c]);
             }
+    free(kb);
     free(buf);
     return 0;
 }

@@ -36,7 +36,7 @@ class OracleParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_float) for n in
                 ("sigma", "dt", "mu", "lambda1", "lambda2", "nu", "eps", "sigma2")] + \
                [("boundary", ctypes.c_int32), ("mag_form", ctypes.c_int32), ("arith", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("data_term", ctypes.c_int32)]
 
 
 _lib = None
@@ -75,9 +75,9 @@ def lib():
 
 
 def params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=None, nu=65.025, eps=0.2, sigma2=0.0,
-           boundary=0, mag_form=0, arith=0) -> OracleParams:
+           boundary=0, mag_form=0, arith=0, data_term=0) -> OracleParams:
     return OracleParams(sigma, dt, mu, lambda1, lambda1 if lambda2 is None else lambda2, nu, eps, sigma2,
-                        boundary, mag_form, arith, 0)
+                        boundary, mag_form, arith, data_term)
 
 
 def _f32(a):

@@ -39,10 +39,13 @@ __device__ __forceinline__ float atan_portable(float x) {
     return copysignf(res, x);
 }
 
-// H = 0.5 (1 + (2/pi) atan(phi/eps)), CUDA_RSF/kernel.cu:258-259.
+// H = 0.5 (1 + (2/pi) atan(phi/eps)), CUDA_RSF/kernel.cu:258-259.  With
+// eps = 1 (a launch-wide value) phi / eps is phi itself, exactly.
 template <Arith A>
 __device__ __forceinline__ float heaviside(float phi, float eps) {
-    const float q = __fdiv_rn(phi, eps);
+    float q;
+    if (eps == 1.0f) q = phi;
+    else q = __fdiv_rn(phi, eps);
     if constexpr (A == Arith::Reference) {
         const float a = atanf(q);
         const double v = __dmul_rn(0.5, __fma_rn(2.0 / 3.14159265358979323846, (double)a, 1.0));
@@ -59,10 +62,15 @@ __device__ __forceinline__ float heaviside(float phi, float eps) {
     }
 }
 
-// delta = (1/pi) eps / (eps^2 + phi^2), CUDA_RSF/kernel.cu:275-276.
+// delta = (1/pi) eps / (eps^2 + phi^2), CUDA_RSF/kernel.cu:275-276.  With
+// eps = 1 the quotient is the correctly rounded reciprocal of the
+// denominator, which __frcp_rn returns with fewer instructions.
 template <Arith A>
 __device__ __forceinline__ float dirac(float phi, float eps) {
-    const float q = __fdiv_rn(eps, __fmaf_rn(phi, phi, __fmul_rn(eps, eps)));
+    const float den = __fmaf_rn(phi, phi, __fmul_rn(eps, eps));
+    float q;
+    if (eps == 1.0f) q = __frcp_rn(den);
+    else q = __fdiv_rn(eps, den);
     if constexpr (A == Arith::Reference) {
         return __double2float_rn(__dmul_rn(1.0 / 3.14159265358979323846, (double)q));
     } else {

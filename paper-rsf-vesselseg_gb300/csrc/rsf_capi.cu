@@ -47,8 +47,9 @@ struct rsf_workspace {
     float *pool_phi2 = nullptr;  // second level-set buffer, max_voxels
     float *pool_x = nullptr;     // x-pass fields, 4 * max_voxels
     float *pool_y = nullptr;     // y-pass fields, 4 * max_voxels
+    float *pool_g = nullptr;     // expanded data term's x-blurred fields, 4 * max_voxels (first use)
     SubVolDev *d_svs = nullptr;
-    int *d_pre = nullptr;        // NKERN * (max_subvols + 1)
+    int *d_pre = nullptr;        // NPRE * (max_subvols + 1)
     unsigned char *d_maps = nullptr;  // TMA maps of the pair planes, max_subvols * TMAP_BYTES
     unsigned *d_flag = nullptr;
     // Pinned staging of the table, kStages slots used in turn: a call waits
@@ -56,7 +57,7 @@ struct rsf_workspace {
     // calls do not make the host wait for the device.
     static constexpr int kStages = 4;
     SubVolDev *h_svs = nullptr;  // kStages * max_subvols
-    int *h_pre = nullptr;        // kStages * NKERN * (max_subvols + 1)
+    int *h_pre = nullptr;        // kStages * NPRE * (max_subvols + 1)
     unsigned char *h_maps = nullptr;  // kStages * max_subvols * TMAP_BYTES
     cudaEvent_t table_ev[kStages] = {};
     bool table_pending[kStages] = {};
@@ -69,7 +70,7 @@ struct rsf_workspace {
             table_pending[stage] = false;
         }
         *svs = h_svs + (size_t)stage * max_subvols;
-        *pre = h_pre + (size_t)stage * rsf::NKERN * ((size_t)max_subvols + 1);
+        *pre = h_pre + (size_t)stage * rsf::NPRE * ((size_t)max_subvols + 1);
         *maps = h_maps + (size_t)stage * max_subvols * rsf::TMAP_BYTES;
         return cudaSuccess;
     }
@@ -187,7 +188,7 @@ rsf_status rsf_gaussian_taps(float sigma, float *taps, int cap, int *k_out) {
 size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols) {
     const size_t v = (size_t)std::max<int64_t>(max_voxels, 0);
     const size_t n = (size_t)std::max<int32_t>(max_subvols, 1);
-    return v * sizeof(float) * 9 + n * (sizeof(SubVolDev) + rsf::TMAP_BYTES) + rsf::NKERN * (n + 1) * sizeof(int) +
+    return v * sizeof(float) * 9 + n * (sizeof(SubVolDev) + rsf::TMAP_BYTES) + rsf::NPRE * (n + 1) * sizeof(int) +
            256;
 }
 
@@ -201,6 +202,7 @@ static void ws_free(rsf_workspace *ws) {
     cudaFree(ws->pool_phi2);
     cudaFree(ws->pool_x);
     cudaFree(ws->pool_y);
+    cudaFree(ws->pool_g);
     cudaFree(ws->d_svs);
     cudaFree(ws->d_pre);
     cudaFree(ws->d_maps);
@@ -240,13 +242,13 @@ rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_wor
     alloc((void **)&ws->pool_x, 4 * v * sizeof(float));
     alloc((void **)&ws->pool_y, 4 * v * sizeof(float));
     alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
-    alloc((void **)&ws->d_pre, rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
+    alloc((void **)&ws->d_pre, rsf::NPRE * ((size_t)max_subvols + 1) * sizeof(int));
     alloc((void **)&ws->d_maps, (size_t)max_subvols * rsf::TMAP_BYTES);
     alloc((void **)&ws->d_flag, 256);
     const size_t ns = rsf_workspace::kStages;
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, ns * (size_t)max_subvols * sizeof(SubVolDev));
     if (e == cudaSuccess)
-        e = cudaMallocHost((void **)&ws->h_pre, ns * rsf::NKERN * ((size_t)max_subvols + 1) * sizeof(int));
+        e = cudaMallocHost((void **)&ws->h_pre, ns * rsf::NPRE * ((size_t)max_subvols + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_maps, ns * (size_t)max_subvols * rsf::TMAP_BYTES);
     for (size_t i = 0; i < ns && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&ws->table_ev[i], cudaEventDisableTiming);
@@ -288,6 +290,10 @@ rsf_status check_params(const rsf_params *p, int *k, float *taps) {
         return fail(RSF_ERR_INVALID_ARGUMENT, "unknown boundary mode");
     if (p->arith != RSF_ARITH_PORTABLE && p->arith != RSF_ARITH_REFERENCE)
         return fail(RSF_ERR_INVALID_ARGUMENT, "unknown arithmetic mode");
+    if (p->data_term != RSF_DATA_TERM_REFERENCE && p->data_term != RSF_DATA_TERM_GAUSSIAN)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "unknown data term");
+    if (p->data_term == RSF_DATA_TERM_GAUSSIAN && p->sigma2 >= 1.0f)
+        return fail(RSF_ERR_UNSUPPORTED, "the Gaussian data term takes no box window (sigma2 < 1)");
     return rsf_gaussian_taps(p->sigma, taps, rsf::MAXK, k);
 }
 
@@ -299,9 +305,10 @@ rsf_status check_shape(int64_t W, int64_t H, int64_t L) {
 }
 
 // Lays out a batch in the workspace pools and uploads the table.
-rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, int box,
-                   rsf_dtype dtype, const float *const *phi_out_override, int totals[rsf::NKERN],
+rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, int kspec, int box, int gauss,
+                   rsf_dtype dtype, const float *const *phi_out_override, int totals[rsf::NPRE],
                    rsf::LaunchShape *shape, cudaStream_t st) {
+    const bool full_data = box > 0 || gauss;
     if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
     if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
@@ -326,10 +333,10 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         whl[3 * i + 1] = (int)svs[i].H;
         whl[3 * i + 2] = (int)svs[i].L;
     }
-    *shape = rsf::choose_shape(whl.data(), n, k, kspec);
+    *shape = rsf::choose_shape(whl.data(), n, k, kspec, gauss);
     const int n1 = n + 1;
     int *pre = h_pre;
-    for (int j = 0; j < rsf::NKERN; j++) pre[j * n1] = 0;
+    for (int j = 0; j < rsf::NPRE; j++) pre[j * n1] = 0;
     size_t off_v = 0, off_x = 0, off_y = 0;
     for (int i = 0; i < n; i++) {
         SubVolDev d;
@@ -338,7 +345,7 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         d.H = (int)svs[i].H;
         d.L = (int)svs[i].L;
         rsf::valid_extents(d.W, d.H, d.L, k, d.Wv, d.Hv, d.Lv, d.Wp);
-        int tiles[rsf::NKERN];
+        int tiles[rsf::NPRE];
         rsf::tile_counts(d, kspec, *shape, tiles);
         const size_t nv = (size_t)d.W * d.H * d.L;
         d.phi[0] = svs[i].phi;
@@ -348,16 +355,18 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         d.db = d.xb;  // the data factor reuses the x-pass storage
         d.yb = ws->pool_y + off_y;
         off_v += nv;
-        // x-pass slot: the four x-pass fields, or with the box e-term f_out,
-        // f_in of the valid region followed by the data factor of every voxel
+        // x-pass slot: the four x-pass fields, or with the box e-term or the
+        // expanded data term f_out, f_in of the valid region followed by the
+        // data factor of every voxel (the expanded term's blurred fields use
+        // the same offsets in pool_g)
         // (rounded up to 4 floats for the vector accesses).  Both are at most
         // 4 W H L floats (Wp < W since k >= 5), so the pool of 4 max_voxels
         // floats holds every batch that passes the voxel check above.
         size_t slot_x = 4 * (size_t)d.Wp * d.H * d.L;
-        if (box > 0) slot_x = std::max(slot_x, (2 * (size_t)d.Wp * d.Hv * d.Lv + nv + 3) & ~(size_t)3);
+        if (full_data) slot_x = std::max(slot_x, (2 * (size_t)d.Wp * d.Hv * d.Lv + nv + 3) & ~(size_t)3);
         off_x += slot_x;
         off_y += 4 * (size_t)d.Wp * d.Hv * d.L;
-        for (int j = 0; j < rsf::NKERN; j++) {
+        for (int j = 0; j < rsf::NPRE; j++) {
             const int64_t next = (int64_t)pre[j * n1 + i] + tiles[j];
             if (next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");
             pre[j * n1 + i + 1] = (int)next;
@@ -366,10 +375,10 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         if (shape->zt && d.Wv > 0 && !rsf::encode_pair_map(h_maps + (size_t)i * rsf::TMAP_BYTES, d))
             return fail(RSF_ERR_CUDA, "TMA tensor map encoding of the pair planes failed");
     }
-    for (int j = 0; j < rsf::NKERN; j++) totals[j] = pre[j * n1 + n];
+    for (int j = 0; j < rsf::NPRE; j++) totals[j] = pre[j * n1 + n];
     cudaError_t e = cudaMemcpyAsync(ws->d_svs, h_svs, (size_t)n * sizeof(SubVolDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ws->d_pre, h_pre, rsf::NKERN * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(ws->d_pre, h_pre, rsf::NPRE * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && shape->zt)
         e = cudaMemcpyAsync(ws->d_maps, h_maps, (size_t)n * rsf::TMAP_BYTES, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = ws->mark_stage(st);
@@ -402,7 +411,34 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.zc = sh.zc;
     c.ymaps = sh.zt ? maps : nullptr;
     c.box = (int)p->sigma2;
+    c.gauss = p->data_term == RSF_DATA_TERM_GAUSSIAN;
+    c.full_data = c.box > 0 || c.gauss;
+    // K*1: the valid correlation of ones in the blur's own order (fused
+    // multiply-adds from +0 over ascending taps, x, then y, then z)
+    float sx = 0.0f, sy = 0.0f, s3 = 0.0f;
+    for (int i = 0; i < k; i++) sx = std::fma(1.0f, taps[i], sx);
+    for (int i = 0; i < k; i++) sy = std::fma(sx, taps[i], sy);
+    for (int i = 0; i < k; i++) s3 = std::fma(sy, taps[i], s3);
+    c.s3 = s3;
+    c.gdelta = 0;
     return c;
+}
+
+// The expanded data term's scratch (4 floats per voxel of the workspace's
+// capacity), allocated on its first use; returns the offset of its slots
+// from the x-pass pool's.
+rsf_status gauss_pool(rsf_workspace *ws, ptrdiff_t *delta) {
+    if (!ws->pool_g) {
+        cudaError_t e = cudaMalloc((void **)&ws->pool_g, 4 * (size_t)ws->max_voxels * sizeof(float));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ws->pool_g = nullptr;
+            return fail(RSF_ERR_NO_MEMORY, "allocation of the Gaussian data term's scratch failed");
+        }
+        ws->bytes += 4 * (size_t)ws->max_voxels * sizeof(float);
+    }
+    *delta = ws->pool_g - ws->pool_x;
+    return RSF_OK;
 }
 
 // Copies the second buffer back into the caller's phi after an odd number
@@ -461,13 +497,15 @@ rsf_status run(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype, const rs
     int k = 0;
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
-    int tot[rsf::NKERN];
+    int tot[rsf::NPRE];
     rsf::LaunchShape sh;
-    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2), (int)p->sigma2, dtype, nullptr, tot,
-                &sh, st);
+    const int gauss = p->data_term == RSF_DATA_TERM_GAUSSIAN;
+    s = prepare(ws, svs, n, k, rsf::kernel_k(k, p->arith, false, (int)p->sigma2, gauss), (int)p->sigma2, gauss, dtype,
+                nullptr, tot, &sh, st);
     if (s != RSF_OK) return s;
     if (iters == 0) return RSF_OK;
-    const StepConst c = make_const(p, k, taps, dtype, n, sh, ws->d_maps);
+    StepConst c = make_const(p, k, taps, dtype, n, sh, ws->d_maps);
+    if (gauss && (s = gauss_pool(ws, &c.gdelta)) != RSF_OK) return s;
     if (ws->timing) {
         s = timing_events(ws, iters, tot);
         if (s != RSF_OK) return s;
@@ -577,12 +615,14 @@ rsf_status rsf_step_debug(rsf_workspace *ws, const rsf_params *p, const void *im
     if (s != RSF_OK) return s;
     rsf_subvol sv = {const_cast<float *>(phi), image, W, H, L};
     const float *outs[1] = {phi_out};
-    int tot[rsf::NKERN];
+    int tot[rsf::NPRE];
     rsf::LaunchShape sh;
     cudaStream_t st = (cudaStream_t)stream;
-    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), (int)p->sigma2, dtype, outs, tot, &sh, st);
+    const int gauss = p->data_term == RSF_DATA_TERM_GAUSSIAN;
+    s = prepare(ws, &sv, 1, k, rsf::kernel_k(k, p->arith, true), (int)p->sigma2, gauss, dtype, outs, tot, &sh, st);
     if (s != RSF_OK) return s;
-    const StepConst c = make_const(p, k, taps, dtype, 1, sh, ws->d_maps);
+    StepConst c = make_const(p, k, taps, dtype, 1, sh, ws->d_maps);
+    if (gauss && (s = gauss_pool(ws, &c.gdelta)) != RSF_OK) return s;
     const rsf::DebugOut dbg = {fields, (int64_t)W * H * L};
     cudaError_t e = rsf::launch_step(ws->d_svs, ws->d_pre, tot, c, 0, p->arith, ws->d_flag, &dbg, st);
     return e == cudaSuccess ? RSF_OK : cuda_fail(e, "debug step");
@@ -617,6 +657,8 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
     if (s != RSF_OK) return s;
     if ((s = check_shape(W, H, L)) != RSF_OK) return s;
     if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the box e-term (sigma2 >= 1) is not implemented");
+    if (p->data_term != RSF_DATA_TERM_REFERENCE)
+        return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the Gaussian data term is not implemented");
     // the stencil adjoint runs on 3-D grids: one z plane per grid row, 8 y per block
     if (L > 65535 || H > 65535 * 8) return fail(RSF_ERR_SHAPE, "the adjoint supports L <= 65535 and H <= 524280");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");

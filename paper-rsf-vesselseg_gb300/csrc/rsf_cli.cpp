@@ -53,6 +53,7 @@ const Option kOptions[] = {
     {"threshold", true, "13", "seed level: voxels with seed > threshold are inside"},
     {"boundary", true, "reference", "derivative boundary rule: reference | clamp"},
     {"arith", true, "portable", "arithmetic: portable (bit-exact with the CPU oracle) | reference"},
+    {"data-term", true, "reference", "data term: reference ((I - f)^2 as kernel.cu) | gaussian (expanded RSF form)"},
     {"device", true, "0", "CUDA device ordinal"},
     {"quiet", false, nullptr, "one timing line for the whole evolution instead of one per step"},
 };
@@ -194,6 +195,13 @@ int main(int argc, char **argv) {
     else if (bnd == "clamp") p.boundary = RSF_BOUNDARY_CLAMP;
     else {
         std::fprintf(stderr, "rsf3d: --boundary must be reference or clamp\n");
+        return 2;
+    }
+    const std::string &dterm = value[idx("data-term")];
+    if (dterm == "reference") p.data_term = RSF_DATA_TERM_REFERENCE;
+    else if (dterm == "gaussian") p.data_term = RSF_DATA_TERM_GAUSSIAN;
+    else {
+        std::fprintf(stderr, "rsf3d: --data-term must be reference or gaussian\n");
         return 2;
     }
     if (arith == "portable") p.arith = RSF_ARITH_PORTABLE;

@@ -1,6 +1,7 @@
 // rsf_internal.h -- data structures shared by the kernels and the C ABI layer.
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 namespace rsf {
@@ -23,7 +24,6 @@ constexpr int ST_ZC = 64;      // stencil: planes per block (32 when that gives 
 // The x-pass lane width (outputs per lane) is chosen per launch from these.
 constexpr int XB_CHOICES[2] = {5, 9};
 
-
 // One sub-volume as the kernels see it.
 //   xb: x-pass fields, each Wp x H x L   (row stride Wp)
 //   yb: y-pass fields, each Wp x Hv x L
@@ -32,9 +32,9 @@ constexpr int XB_CHOICES[2] = {5, 9};
 //   separate float planes (H, 1-H, I H, I (1-H)).
 //   db: data factor lambda (e_out - e_in) of the valid region, Wp x Hv x Lv;
 //       it reuses the x-pass storage, which is dead once the y-pass has run.
-//       With the box e-term it holds f_out and f_in of the valid region
-//       (Wp x Hv x Lv each) followed by the data factor of every voxel
-//       (W x H x L).
+//       With the box e-term or the expanded data term it holds f_out and
+//       f_in of the valid region (Wp x Hv x Lv each) followed by the data
+//       factor of every voxel (W x H x L).
 struct SubVolDev {
     float *phi[2];       // ping-pong level-set buffers
     const void *img;     // image, uint8 or float32
@@ -61,6 +61,10 @@ struct StepConst {
     int pairs;      // 1: x/y fields in float2 pair planes (specialised tap counts)
     int zc;         // stencil planes per block for this launch
     int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
+    int gauss;      // 1: expanded Gaussian data term (rsf_gauss.cu)
+    int full_data;  // box or gauss: the z-pass stores the fits, the data factor of every voxel follows them
+    float s3;       // gauss: the valid correlation of ones, K*1
+    ptrdiff_t gdelta;  // gauss: offset (floats) of the scratch G from xb
     const void *ymaps;  // per sub-volume TMA map of the y-pass pair planes (TMAP_BYTES each), or null
 };
 
@@ -79,7 +83,13 @@ struct DebugOut {
     int64_t n;
 };
 
-constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil
+constexpr int NKERN = 4;  // x-pass, y-pass, z-pass, stencil (timed separately)
+// Block prefix arrays per batch: the NKERN kernels, then the expanded
+// data term's gauss_x, second y-pass, gauss_z and gauss_border.
+constexpr int NPRE = NKERN + 4;
+constexpr int GX_T = 128;  // gauss_x: threads per block
+constexpr int GX_NB = 4;   // gauss_x: x-outputs per thread
+constexpr int GB_T = 256;  // gauss_border: voxels per block
 
 // Bits of the per-workspace error flag the kernels set.
 constexpr unsigned kFlagNonFinite = 1u;  // a non-finite value was written to phi
@@ -90,25 +100,26 @@ constexpr unsigned kFlagAdjointNonFinite = 4u;  // rsf_step_adjoint produced a n
 // debug step, the reference arithmetic and the box e-term use the
 // run-time-k kernels.
 inline bool is_specialised(int k) { return k == 21 || k == 29 || k == 35; }
-inline int kernel_k(int k, int arith, bool debug, int box = 0) {
-    return (is_specialised(k) && arith == 0 && !debug && box == 0) ? k : 0;
+inline int kernel_k(int k, int arith, bool debug, int box = 0, int gauss = 0) {
+    return (is_specialised(k) && arith == 0 && !debug && box == 0 && gauss == 0) ? k : 0;
 }
 // Specialised tap counts whose z-pass can run fed by TMA (its image prefetch
 // ring depth divides k).
 inline bool tma_z(int kspec) { return kspec == 21 || kspec == 35; }
 constexpr int MAX_BOX = 8;  // largest e-term box radius
 
-// Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
 // Per-launch tile shapes of a batch.
 struct LaunchShape {
-    int xb_w;   // x-pass outputs per lane (separate passes)
+    int xb_w;   // x-pass outputs per lane
     int pairs;  // 1: x/y fields in float2 pair planes (specialised tap counts)
-    int zt;     // 1: the fused path's z-pass loads planes with TMA (needs a map per sub-volume)
+    int zt;     // 1: the z-pass loads planes with TMA (needs a map per sub-volume)
     int zc;     // stencil planes per block
+    int gauss;  // 1: the expanded data term's kernels run (tiles NKERN .. NPRE - 1)
 };
 // whl: W, H, L of each sub-volume; kspec: kernel_k().
-LaunchShape choose_shape(const int *whl, int n, int k, int kspec);
-void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NKERN]);
+LaunchShape choose_shape(const int *whl, int n, int k, int kspec, int gauss = 0);
+// Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
+void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NPRE]);
 int choose_xb(const int *Wv, int n);
 int choose_zc(const int *whl, int n);  // whl: W, H, L of each sub-volume
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
@@ -146,6 +157,10 @@ cudaError_t launch_ztpass_21(const SubVolDev *, const int *, int, const StepCons
 cudaError_t launch_ztpass_35(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
 cudaError_t launch_stencil(const SubVolDev *, const int *, int, const StepConst &, int parity, int arith,
                            unsigned *flag, const DebugOut *dbg, cudaStream_t);
+// Expanded data term (c.gauss): its four kernels after the z-pass; pre holds
+// NPRE prefix arrays of n1 entries, tot their totals.
+cudaError_t launch_gauss(const SubVolDev *, const int *pre, int n1, const int *tot, const StepConst &,
+                         const DebugOut *dbg, cudaStream_t);
 // Box e-term (c.box >= 1): data factor of every voxel, stencil tiling.
 cudaError_t launch_box(const SubVolDev *, const int *, int, const StepConst &, const DebugOut *dbg, cudaStream_t);
 // Reverse-mode derivative of one step (rsf_adjoint.cu); scratch from the

@@ -456,6 +456,8 @@ __global__ void __launch_bounds__(YP_COLS) ypass_kernel(const SubVolDev *__restr
     stream_axis<K>(rg, c, emit);
 }
 
+// U = 1: the second (expanded data term) pass, reading the scratch G at
+// xb + gdelta instead of the x-pass fields.
 template <int U = 0>
 __global__ void __launch_bounds__(YB_TX) ypass_generic_kernel(const SubVolDev *__restrict__ svs,
                                                               const int *__restrict__ pre, const StepConst c) {
@@ -476,7 +478,7 @@ __global__ void __launch_bounds__(YB_TX) ypass_generic_kernel(const SubVolDev *_
     const int x = tx * YB_TX + threadIdx.x;
     if (x >= s.Wv) return;
     const int y0 = ty * YB_YB;
-    const float *src = s.xb + f * ((size_t)s.Wp * s.H * s.L) + (size_t)z * s.H * s.Wp + x;
+    const float *src = (U ? s.xb + c.gdelta : s.xb) + f * ((size_t)s.Wp * s.H * s.L) + (size_t)z * s.H * s.Wp + x;
     float *dst = s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)z * s.Hv * s.Wp + x;
     float acc[YB_YB];
     conv_block_rt<YB_YB>(src, (size_t)s.Wp, y0, s.H, taps_s, c.k, acc);
@@ -640,7 +642,7 @@ __global__ void __launch_bounds__(ZB_TX) zpass_generic_kernel(const SubVolDev *_
         const int o = z0 + m;
         if (o >= s.Lv) break;
         const size_t vi = ((size_t)(o + r) * s.H + (y + r)) * s.W + (x + r);
-        if (c.box > 0) {  // the box kernel forms e from the fits
+        if (c.full_data) {  // the box or expanded data-term kernels form e from the fits
             const size_t di = ((size_t)o * s.Hv + y) * s.Wp + x;
             s.db[di] = fo[m];
             s.db[(size_t)s.Wp * s.Hv * s.Lv + di] = fi[m];
@@ -833,7 +835,7 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
             if (!inside) {
                 dbg.f[0 * dbg.n + vi] = 1.0f;
                 dbg.f[1 * dbg.n + vi] = 1.0f;
-                if (c.box == 0) {  // the box kernel wrote e everywhere
+                if (!c.full_data) {  // else the data-term kernels wrote e everywhere
                     const float I = load_img(k.s->img, vi, c.img_f32);
                     const float d = __fsub_rn(I, 1.0f);
                     dbg.f[2 * dbg.n + vi] = __fmul_rn(d, d);
@@ -1020,7 +1022,7 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
                    k.z0 >= r && k.z1 - 1 < k.L - r;
     k.dplane = (size_t)s.Wp * s.Hv;
     k.dcol = k.inside_xy ? s.db + (size_t)(k.y - r) * s.Wp + (k.x - r) : s.db;
-    if (c.box > 0) {  // every voxel's data factor comes from the box kernel
+    if (c.full_data) {  // every voxel's data factor comes from the box or expanded data-term kernels
         k.blk_inside = true;
         k.dplane = k.WH;
         k.dcol = s.db + 2 * (size_t)s.Wp * s.Hv * s.Lv + k.col + (size_t)r * k.WH;

@@ -97,6 +97,8 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
         if (!std::isfinite(v)) return fail(RSF_ERR_INVALID_ARGUMENT, "rsf_evolve_noalloc: non-finite parameter");
     if (!(p->eps > 0.0f) || p->sigma2 < 0.0f) return fail(RSF_ERR_INVALID_ARGUMENT, "rsf_evolve_noalloc: bad eps or sigma2");
     if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "rsf_evolve_noalloc: box e-term is not implemented");
+    if (p->data_term != RSF_DATA_TERM_REFERENCE)
+        return fail(RSF_ERR_UNSUPPORTED, "rsf_evolve_noalloc: the Gaussian data term is not implemented");
     if ((p->boundary != RSF_BOUNDARY_REFERENCE && p->boundary != RSF_BOUNDARY_CLAMP) ||
         (p->arith != RSF_ARITH_PORTABLE && p->arith != RSF_ARITH_REFERENCE))
         return fail(RSF_ERR_INVALID_ARGUMENT, "rsf_evolve_noalloc: unknown boundary or arithmetic mode");
@@ -133,10 +135,10 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     const int whl[3] = {d.W, d.H, d.L};
     const int kspec = rsf::kernel_k(k, p->arith, false);
     const rsf::LaunchShape sh = rsf::choose_shape(whl, 1, k, kspec);
-    int tiles[rsf::NKERN];
+    int tiles[rsf::NPRE];
     rsf::tile_counts(d, kspec, sh, tiles);
-    int pre[2 * rsf::NKERN];  // per kernel: {0, tiles}
-    for (int j = 0; j < rsf::NKERN; j++) {
+    int pre[2 * rsf::NPRE];  // per kernel: {0, tiles}
+    for (int j = 0; j < rsf::NPRE; j++) {
         pre[2 * j] = 0;
         pre[2 * j + 1] = tiles[j];
     }

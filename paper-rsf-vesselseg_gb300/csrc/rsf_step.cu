@@ -67,7 +67,7 @@ int choose_zc(const int *whl, int n) {
     return blocks >= 4LL * 2 * sm_count() ? ST_ZC : ST_ZC / 2;
 }
 
-LaunchShape choose_shape(const int *whl, int n, int k, int kspec) {
+LaunchShape choose_shape(const int *whl, int n, int k, int kspec, int gauss) {
     LaunchShape sh;
     std::vector<int> wv((size_t)n);
     for (int i = 0; i < n; i++) {
@@ -79,6 +79,7 @@ LaunchShape choose_shape(const int *whl, int n, int k, int kspec) {
     sh.pairs = kspec > 0 ? 1 : 0;
     sh.zt = tma_z(kspec) && tma_z_requested() && tensor_maps_available() ? 1 : 0;
     sh.zc = choose_zc(whl, n);
+    sh.gauss = gauss;
     return sh;
 }
 
@@ -130,7 +131,7 @@ bool encode_pair_map(void *out, const SubVolDev &d) {
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NKERN]) {
+void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NPRE]) {
     const bool valid = d.Wv > 0;
     const int xt = 32 * sh.xb_w, zc = sh.zc;
     tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L : 0;
@@ -142,6 +143,12 @@ void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles
     else if (kspec == 0) tiles[2] = ((d.Wv + ZB_TX - 1) / ZB_TX) * ((d.Lv + ZB_ZB - 1) / ZB_ZB) * d.Hv;
     else tiles[2] = ((d.Wv + 2 * ZP_PAIRS - 1) / (2 * ZP_PAIRS)) * d.Hv;
     tiles[3] = ((d.W + ST_OX - 1) / ST_OX) * ((d.H + ST_OY - 1) / ST_OY) * ((d.L + zc - 1) / zc);
+    // expanded data term: gauss_x, second y-pass, gauss_z, gauss_border
+    const bool g = sh.gauss != 0;
+    tiles[NKERN] = g && valid ? ((d.Wv + GX_T * GX_NB - 1) / (GX_T * GX_NB)) * d.H * d.L : 0;
+    tiles[NKERN + 1] = g && valid ? ((d.Wv + YB_TX - 1) / YB_TX) * ((d.Hv + YB_YB - 1) / YB_YB) * 4 * d.L : 0;
+    tiles[NKERN + 2] = g && valid ? ((d.Wv + ZB_TX - 1) / ZB_TX) * ((d.Lv + ZB_ZB - 1) / ZB_ZB) * d.Hv : 0;
+    tiles[NKERN + 3] = g ? (int)(((long long)d.W * d.H * d.L + GB_T - 1) / GB_T) : 0;
 }
 
 // Raises the dynamic shared-memory limit of the x-pass instantiations on the
@@ -159,7 +166,7 @@ cudaError_t configure_device() {
 cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, const StepConst &c, int parity,
                         int arith, unsigned *flag, const DebugOut *dbg, cudaStream_t st, cudaEvent_t *ev) {
     const int n1 = c.nsv + 1;
-    const int kspec = kernel_k(c.k, arith, dbg != nullptr, c.box);
+    const int kspec = kernel_k(c.k, arith, dbg != nullptr, c.box, c.gauss);
     cudaError_t e = cudaSuccess;
     // Inside a stream capture a plain record only orders streams; an external
     // record becomes an event record node of the graph.  Outside a capture
@@ -200,6 +207,10 @@ cudaError_t launch_step(const SubVolDev *svs, const int *pre, const int *tot, co
             case 35: e = launch_zpass_35(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
             default: e = launch_zpass_0(svs, pre + 2 * n1, tot[2], c, dbg, st); break;
         }
+        if (e != cudaSuccess) return e;
+    }
+    if (c.gauss) {
+        e = launch_gauss(svs, pre, n1, tot, c, dbg, st);
         if (e != cudaSuccess) return e;
     }
     if (c.box > 0 && tot[3] > 0) {

@@ -24,7 +24,7 @@ class RsfParams(ctypes.Structure):
     _fields_ = [("sigma", ctypes.c_float), ("dt", ctypes.c_float), ("mu", ctypes.c_float),
                 ("lambda1", ctypes.c_float), ("lambda2", ctypes.c_float), ("nu", ctypes.c_float),
                 ("eps", ctypes.c_float), ("sigma2", ctypes.c_float), ("boundary", ctypes.c_int32),
-                ("arith", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("arith", ctypes.c_int32), ("data_term", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 class RsfSubvol(ctypes.Structure):

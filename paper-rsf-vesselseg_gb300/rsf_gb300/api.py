@@ -4,7 +4,8 @@ evolution entry points over torch CUDA tensors or NumPy host arrays.
 The reference's executable takes --sigma --t --dt --meu --e --v --sigma2
 (CUDA_RSF/main.cpp:88-102); `Params` keeps those meanings (and defaults) and
 adds the knobs the reference hard-codes: eps (kernel.cu:258,275), separate
-lambda1/lambda2, the x = 0 boundary rule and the arithmetic definition.
+lambda1/lambda2, the x = 0 boundary rule and the arithmetic definition, and
+one mode of this project's own: the expanded Gaussian data term.
 """
 from __future__ import annotations
 
@@ -29,6 +30,7 @@ class Params:
     sigma2: float = 0.0     # --sigma2
     boundary: str = "reference"  # or "clamp"
     arith: str = "portable"      # or "reference"
+    data_term: str = "reference"  # or "gaussian" (expanded RSF data term, no counterpart in the reference)
 
     def to_c(self) -> RsfParams:
         p = RsfParams()
@@ -37,6 +39,7 @@ class Params:
         p.eps, p.sigma2 = self.eps, self.sigma2
         p.boundary = {"reference": 0, "clamp": 1}[self.boundary]
         p.arith = {"portable": 0, "reference": 1}[self.arith]
+        p.data_term = {"reference": 0, "gaussian": 1}[self.data_term]
         return p
 
     @classmethod

@@ -32,7 +32,8 @@ CU_UNITS = ([(f"rsf_{fam}.cu", f"rsf_{fam}_k{k}", [f"-DRSF_K={k}"]) for fam in (
             + [("rsf_stencil.cu", "rsf_stencil", []), ("rsf_step.cu", "rsf_step", []),
                ("rsf_capi.cu", "rsf_capi", []), ("rsf_noalloc.cu", "rsf_noalloc", []),
                ("rsf_sdf.cu", "rsf_sdf", []), ("rsf_adjoint.cu", "rsf_adjoint", []),
-               ("rsf_reassemble.cu", "rsf_reassemble", []), ("rsf_copy.cu", "rsf_copy", [])])
+               ("rsf_reassemble.cu", "rsf_reassemble", []), ("rsf_copy.cu", "rsf_copy", []),
+               ("rsf_gauss.cu", "rsf_gauss", [])])
 CLI_SOURCES = ["rsf_cli.cpp", "npy_io.cpp"]
 
 

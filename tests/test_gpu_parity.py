@@ -292,3 +292,63 @@ def test_tma_z_pass_bit_exact(sigma, orc, ws_big, cuda, monkeypatch):
             assert _bits_equal(a, b), f"{img.shape} {dtype}: TMA and streaming z-pass differ"
             want = orc.evolve(phi0, img.astype(np.float32), _oracle_params(orc, p), 3)
             assert _bits_equal(a, want), f"{img.shape} {dtype}: {_diff_report(a, want)}"
+
+
+GAUSS_CASES = [
+    # shape, sigma, lambda1, lambda2, dtype, iters
+    ((26, 28, 30), 1.5, 1.0, 1.0, "u8", 3),      # k = 11
+    ((40, 44, 48), 3.0, 1.0, 0.5, "f32", 2),     # k = 21, lambda1 != lambda2
+    ((9, 12, 10), 3.0, 1.0, 1.0, "u8", 2),       # no valid blur region: border form only
+]
+
+
+def _gauss_oracle_params(orc, p):
+    return orc.params(sigma=p.sigma, dt=p.dt, mu=p.mu, lambda1=p.lambda1, lambda2=p.lambda2, nu=p.nu, eps=p.eps,
+                      data_term=1)
+
+
+@pytest.mark.parametrize("case", GAUSS_CASES, ids=lambda c: f"{c[0]}-s{c[1]}-{c[4]}")
+def test_gaussian_data_term_bit_exact(case, orc, ws_big, cuda):
+    """The expanded Gaussian data term (data_term = "gaussian"): evolution,
+    one step's e_out / e_in fields and a batch of all three shapes against the
+    oracle's FP32 restatement, bit for bit.  The mode has no counterpart in
+    the reference, so its parity is pinned to the oracle only."""
+    import torch
+    from rsf_gb300 import Params
+
+    shape, sigma, l1, l2, dtype, iters = case
+    img, phi0, _ = _inputs(shape, seed=41, dtype=dtype)
+    p = Params(sigma=sigma, dt=0.1, mu=1.0, lambda1=l1, lambda2=l2, nu=65.025, eps=1.0, data_term="gaussian")
+    tp = torch.from_numpy(phi0).to(cuda)
+    ws_big.evolve(torch.from_numpy(img).to(cuda), tp, p, iters)
+    ws_big.check()
+    got = tp.cpu().numpy()
+    want = orc.evolve(phi0, img.astype(np.float32), _gauss_oracle_params(orc, p), iters)
+    assert _bits_equal(got, want), _diff_report(got, want)
+    out, fields = ws_big.step_debug(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda), p)
+    want_out, want_fields = orc.step(phi0, img.astype(np.float32), _gauss_oracle_params(orc, p), debug=True)
+    got_fields = fields.cpu().numpy()
+    for i, n in enumerate(["f_out", "f_in", "e_out", "e_in"]):
+        assert _bits_equal(got_fields[i], want_fields[i]), f"{n}: {_diff_report(got_fields[i], want_fields[i])}"
+    assert _bits_equal(out.cpu().numpy(), want_out)
+
+
+def test_gaussian_data_term_batched_and_rejections(orc, ws_big, cuda):
+    import torch
+    from rsf_gb300 import Params, RsfError
+
+    shapes = [(26, 28, 30), (9, 12, 10), (40, 44, 48)]
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=1.0, data_term="gaussian")
+    inputs = [_inputs(s, seed=50 + i)[:2] for i, s in enumerate(shapes)]
+    pairs = [(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda)) for img, phi0 in inputs]
+    ws_big.evolve_batched(pairs, p, 2)
+    ws_big.check()
+    for (img, phi0), (_, b) in zip(inputs, pairs):
+        want = orc.evolve(phi0, img.astype(np.float32), _gauss_oracle_params(orc, p), 2)
+        assert _bits_equal(b.cpu().numpy(), want), f"{img.shape}: {_diff_report(b.cpu().numpy(), want)}"
+    img, phi0 = inputs[0]
+    ti, tp = torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda)
+    with pytest.raises(RsfError, match="sigma2"):
+        ws_big.evolve(ti, tp, Params(sigma=3.0, sigma2=1.0, data_term="gaussian"), 1)
+    with pytest.raises(RsfError, match="Gaussian data term"):
+        ws_big.step_adjoint(ti.float(), tp, tp.clone(), p)

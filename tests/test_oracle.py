@@ -202,3 +202,51 @@ def test_lambda_split_reduces_to_single_e(orc):
 def test_volume_smaller_than_kernel_is_all_border(orc):
     f = np.random.default_rng(8).uniform(0, 1, (9, 10, 11)).astype(f32)
     assert np.all(orc.blur_padded(f, 3.0) == 30.0)
+
+
+def test_gaussian_data_term_matches_its_formula(orc):
+    """The oracle's expanded Gaussian data term (data_term = 1) against the
+    formula evaluated independently with NumPy in float64 from the oracle's
+    own fits: e = I^2 K*1 - 2 I K*f + K*f^2 on the valid region, (I - 1)^2 on
+    the border band; FP32 against FP64 within 1e-5 of max|e|."""
+    from rsf_gb300 import synth
+
+    img, phi0, _ = synth.make_small((26, 28, 30), n_tubes=3, seed=5)
+    I = img.astype(np.float32)
+    p = orc.params(sigma=1.5, eps=1.0, lambda1=1.0, mu=1.0, nu=65.025, dt=0.1, data_term=1)
+    _, fields = orc.step(phi0, I, p, debug=True)
+    fo, fi, eo, ei = (fields[j].astype(np.float64) for j in range(4))
+    g = orc.taps(1.5).astype(np.float64)
+    k, r = len(g), (len(g) - 1) // 2
+
+    def blur_valid(f):
+        out = f
+        for axis in (2, 1, 0):
+            n = out.shape[axis] - k + 1
+            out = sum(g[t] * np.take(out, np.arange(t, t + n), axis=axis) for t in range(k))
+        return out
+
+    s3 = float(np.sum(g)) ** 3
+    sl = tuple(slice(r, n - r) for n in I.shape)
+    Iv = I.astype(np.float64)[sl]
+    for f, e in ((fo, eo), (fi, ei)):
+        want = Iv * Iv * s3 - 2.0 * Iv * blur_valid(f) + blur_valid(f * f)
+        assert np.abs(e[sl] - want).max() <= 1e-5 * np.abs(want).max()
+        border = np.ones(I.shape, bool)
+        border[sl] = False
+        assert np.array_equal(e[border], ((I.astype(np.float64) - 1.0) ** 2)[border])
+    # the two data terms give different evolutions
+    p0 = orc.params(sigma=1.5, eps=1.0, lambda1=1.0, mu=1.0, nu=65.025, dt=0.1, data_term=0)
+    assert not np.array_equal(orc.evolve(phi0, I, p0, 1), orc.evolve(phi0, I, p, 1))
+
+
+def test_gaussian_data_term_fp32_tracks_fp64(orc):
+    from rsf_gb300 import synth
+
+    img, phi0, _ = synth.make_small((30, 32, 34), n_tubes=3, seed=6)
+    I = img.astype(np.float32)
+    p = orc.params(sigma=3.0, eps=1.0, lambda1=1.0, lambda2=0.5, mu=1.0, nu=65.025, dt=0.1, data_term=1)
+    a = orc.evolve(phi0, I, p, 2)
+    b = orc.evolve_f64(phi0.astype(np.float64), I, p, 2)
+    assert float(np.abs(a - b).max()) <= 1e-4 * float(np.abs(b).max())
+    assert float((np.sign(a) == np.sign(b)).mean()) >= 0.9999
