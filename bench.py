@@ -487,6 +487,10 @@ def run_ours(args):
     k = len(gaussian_taps(SIGMA))
     ws = Workspace(total_vox, len(tiles))
     pairs = list(zip(imgs, work))
+    # kernel launch shapes measured on this batch, before the timed region
+    from rsf_gb300 import autotune
+
+    shape = autotune.tune_launch_shape(ws, pairs, p, iters=3)
 
     def step():
         for w, p0 in zip(work, phi0s):
@@ -668,6 +672,9 @@ def run_ours(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "subvolumes": len(tiles), "voxels": total_vox, "iterations": ITERS,
                        "sigma": SIGMA, "taps": k,
+                       "launch_shape": {"xpass_width": shape.xpass_width, "stencil_planes": shape.stencil_planes,
+                                        "z_tma": shape.z_tma, "tuned_ms_per_iteration": {
+                                            f"{a}/{b}/{z}": round(ms, 3) for (a, b, z), ms in shape.table}},
                        "step": f"one {ITERS}-iteration evolution of all {len(tiles)} sub-volumes",
                        "l2": f"inputs larger than L2 (phi {total_vox * 4 / 1e9:.1f} GB, y-pass fields "
                              f"{total_vox * 16 / 1e9:.0f} GB per iteration)",

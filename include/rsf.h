@@ -144,6 +144,16 @@ size_t rsf_workspace_bytes(const rsf_workspace *ws);
 /* Device bytes a workspace for `max_voxels` / `max_subvols` would hold. */
 size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols);
 
+/* Kernel launch shapes for the workspace's later calls, overriding the
+ * per-batch heuristics (0, or -1 for z_tma, restores them): x-pass outputs
+ * per lane (5 or 9), stencil planes per block (32 or 64) and whether the
+ * 21/35-tap z-pass takes its planes through TMA (1) or the streaming ring
+ * (0).  Results do not depend on the choice (every shape is bit-identical);
+ * rsf_gb300.autotune.tune_launch_shape measures them on a batch.  No
+ * counterpart in the reference, whose launch shapes are fixed in kernel.cu. */
+rsf_status rsf_workspace_set_launch_shape(rsf_workspace *ws, int32_t xpass_width, int32_t stencil_planes,
+                                          int32_t z_tma);
+
 /* Evolves one volume in place for `iters` iterations: the device-resident
  * equivalent of the reference's hot loop (main.cpp:222-314).
  * Replaces the per-op host wrappers declared at main.cpp:56-71. */

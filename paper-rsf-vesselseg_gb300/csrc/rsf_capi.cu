@@ -84,6 +84,8 @@ struct rsf_workspace {
     }
     cudaStream_t capture_stream = nullptr;
     size_t bytes = 0;
+    // launch-shape overrides (rsf_workspace_set_launch_shape; 0 / -1: automatic)
+    int force_xb = 0, force_zc = 0, force_zt = -1;
     // host-buffer convenience path (allocated on first use)
     void *stage_img = nullptr;
     float *stage_phi = nullptr;
@@ -274,6 +276,20 @@ rsf_status rsf_workspace_destroy(rsf_workspace *ws) {
 
 size_t rsf_workspace_bytes(const rsf_workspace *ws) { return ws ? ws->bytes : 0; }
 
+rsf_status rsf_workspace_set_launch_shape(rsf_workspace *ws, int32_t xpass_width, int32_t stencil_planes,
+                                          int32_t z_tma) {
+    if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    if (xpass_width != 0 && xpass_width != rsf::XB_CHOICES[0] && xpass_width != rsf::XB_CHOICES[1])
+        return fail(RSF_ERR_INVALID_ARGUMENT, "x-pass width must be 0 (automatic), 5 or 9");
+    if (stencil_planes != 0 && stencil_planes != rsf::ST_ZC && stencil_planes != rsf::ST_ZC / 2)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "stencil planes must be 0 (automatic), 32 or 64");
+    if (z_tma < -1 || z_tma > 1) return fail(RSF_ERR_INVALID_ARGUMENT, "z_tma must be -1 (automatic), 0 or 1");
+    ws->force_xb = xpass_width;
+    ws->force_zc = stencil_planes;
+    ws->force_zt = z_tma;
+    return RSF_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -334,6 +350,9 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         whl[3 * i + 2] = (int)svs[i].L;
     }
     *shape = rsf::choose_shape(whl.data(), n, k, kspec, gauss);
+    if (ws->force_xb) shape->xb_w = ws->force_xb;
+    if (ws->force_zc) shape->zc = ws->force_zc;
+    if (ws->force_zt >= 0) shape->zt = ws->force_zt && rsf::tma_z(kspec) && rsf::tensor_maps_available() ? 1 : 0;
     const int n1 = n + 1;
     int *pre = h_pre;
     for (int j = 0; j < rsf::NPRE; j++) pre[j * n1] = 0;

@@ -58,6 +58,7 @@ SIGNATURES = {
     "rsf_workspace_destroy": (ctypes.c_int, [_P]),
     "rsf_workspace_bytes": (ctypes.c_size_t, [_P]),
     "rsf_workspace_bytes_for": (ctypes.c_size_t, [_I64, _I32]),
+    "rsf_workspace_set_launch_shape": (ctypes.c_int, [_P, _I32, _I32, _I32]),
     "rsf_evolve": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), _P, ctypes.c_int, _P, _I64, _I64, _I64, _I32, _P]),
     "rsf_evolve_batched": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), ctypes.c_int, ctypes.POINTER(RsfSubvol),
                                           _I32, _I32, _P]),

@@ -1,4 +1,5 @@
-"""Tile-shape autotuner for whole-volume evolution.
+"""Autotuners: tile shapes for whole-volume evolution (`tune_cores`) and
+kernel launch shapes for a batch (`tune_launch_shape`).
 
 The batch driver evolves a volume as a grid of cores grown by a halo.  The
 halo is fixed by correctness (it bounds how far missing context reaches a
@@ -114,3 +115,66 @@ def tune_cores(shape: Sequence[int], params: Params, halo: int = 32, dtype: str 
     if timer is None:
         _CACHE[key] = res
     return res
+
+
+# ---------------------------------------------------------------------------
+# Kernel launch shapes.  The kernels take three shape choices per launch: the
+# x-pass lane width (5 or 9 outputs per lane: which wastes fewer outputs past
+# the valid width depends on the batch's row lengths), the stencil's planes
+# per block (64, or 32 for batches too small to fill the GPU several times)
+# and, for 21 and 35 taps, whether the z-pass takes its planes through TMA.
+# The workspace picks them by heuristics; `tune_launch_shape` times every
+# combination on the caller's batch and keeps the fastest.
+# ---------------------------------------------------------------------------
+LAUNCH_CANDIDATES = tuple((xb, zc, zt) for xb in (5, 9) for zc in (64, 32) for zt in (0, 1))
+
+
+@dataclass
+class LaunchShape:
+    xpass_width: int
+    stencil_planes: int
+    z_tma: int
+    ms_per_iteration: float
+    table: List[Tuple[Tuple[int, int, int], float]]
+
+
+def pick_launch_shape(measurements: Sequence[Tuple[Tuple[int, int, int], float]]) -> LaunchShape:
+    """The fastest of (shape, ms per iteration); ties keep the first."""
+    best = min(measurements, key=lambda m: m[1])
+    (xb, zc, zt), ms = best
+    return LaunchShape(xb, zc, zt, ms, list(measurements))
+
+
+def tune_launch_shape(ws: Workspace, pairs, params: Params, iters: int = 4,
+                      candidates: Sequence[Tuple[int, int, int]] = LAUNCH_CANDIDATES,
+                      timer: Optional[Callable[[Tuple[int, int, int]], float]] = None) -> LaunchShape:
+    """Times `iters` batched iterations of `pairs` (image, phi) for every
+    launch shape, restoring each phi between the runs, sets the fastest on
+    `ws` and returns it.  `timer(shape) -> ms per iteration` replaces the
+    device measurement (for tests)."""
+    meas = []
+    if timer is not None:
+        for shape in candidates:
+            meas.append((tuple(shape), float(timer(tuple(shape)))))
+    else:
+        import torch
+
+        starts = [phi.clone() for _, phi in pairs]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for shape in candidates:
+            ws.set_launch_shape(*shape)
+            ws.evolve_batched(pairs, params, 1)  # graph capture and table upload
+            for (_, phi), s0 in zip(pairs, starts):
+                phi.copy_(s0)
+            torch.cuda.synchronize()
+            e0.record()
+            ws.evolve_batched(pairs, params, iters)
+            e1.record()
+            torch.cuda.synchronize()
+            meas.append((tuple(shape), e0.elapsed_time(e1) / iters))
+            for (_, phi), s0 in zip(pairs, starts):
+                phi.copy_(s0)
+        ws.check()
+    best = pick_launch_shape(meas)
+    ws.set_launch_shape(best.xpass_width, best.stencil_planes, best.z_tma)
+    return best

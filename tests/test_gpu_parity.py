@@ -352,3 +352,37 @@ def test_gaussian_data_term_batched_and_rejections(orc, ws_big, cuda):
         ws_big.evolve(ti, tp, Params(sigma=3.0, sigma2=1.0, data_term="gaussian"), 1)
     with pytest.raises(RsfError, match="Gaussian data term"):
         ws_big.step_adjoint(ti.float(), tp, tp.clone(), p)
+
+
+def test_launch_shapes_are_bit_identical_and_autotuned(ws_big, cuda):
+    """Every kernel launch shape (x-pass lane width, stencil planes per
+    block, TMA or streaming z-pass) gives the same bits; the launch-shape
+    autotuner measures them on a batch and leaves the fastest set."""
+    import torch
+    from rsf_gb300 import Params, RsfError, autotune
+
+    shapes = [(40, 44, 48), (64, 33, 70), (9, 9, 9)]
+    p = Params(sigma=3.0, dt=0.1, mu=1.0, lambda1=1.0, lambda2=1.0, nu=65.025, eps=1.0)
+    inputs = [_inputs(s, seed=60 + i)[:2] for i, s in enumerate(shapes)]
+    ref = None
+    try:
+        for shape in autotune.LAUNCH_CANDIDATES:
+            ws_big.set_launch_shape(*shape)
+            pairs = [(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda)) for img, phi0 in inputs]
+            ws_big.evolve_batched(pairs, p, 3)
+            ws_big.check()
+            out = [b.cpu().numpy() for _, b in pairs]
+            if ref is None:
+                ref = out
+            for a, b in zip(out, ref):
+                assert _bits_equal(a, b), f"launch shape {shape} changes the result"
+        with pytest.raises(RsfError):
+            ws_big.set_launch_shape(7, 0, -1)
+        pairs = [(torch.from_numpy(img).to(cuda), torch.from_numpy(phi0).to(cuda)) for img, phi0 in inputs]
+        best = autotune.tune_launch_shape(ws_big, pairs, p, iters=2)
+        assert (best.xpass_width, best.stencil_planes, best.z_tma) in autotune.LAUNCH_CANDIDATES
+        assert best.ms_per_iteration == min(ms for _, ms in best.table)
+        for (_, b), (_, phi0) in zip(pairs, inputs):  # phi restored after the measurements
+            assert torch.equal(b.cpu(), torch.from_numpy(phi0))
+    finally:
+        ws_big.set_launch_shape(0, 0, -1)
