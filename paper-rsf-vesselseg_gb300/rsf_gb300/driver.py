@@ -24,7 +24,7 @@ from typing import List, Sequence
 import numpy as np
 
 from .api import Params, Workspace
-from .tiling import Tile, plan, reassemble_device
+from .tiling import Tile, lpt_shards, plan, reassemble_device
 
 # Device bytes per tile voxel while a chunk evolves: workspace 36, phi 4,
 # image up to 4, seed up to 4.
@@ -60,32 +60,57 @@ def _tile_to_device(src, t: Tile, device):
 
 
 def segment(image, seed, params: Params, iters: int, cores=256, halo: int = 32, mode: str = "core",
-            threshold: float = 13.0, max_chunk_voxels: int | None = None, device="cuda:0", tiles=None):
+            threshold: float = 13.0, max_chunk_voxels: int | None = None, device="cuda:0", tiles=None,
+            distributed: bool = False):
     """Evolved level set of the whole volume as a CUDA float32 tensor (L, H, W).
 
     image: uint8 or float32 (L, H, W) array or CUDA tensor; seed: same shape,
     inside where seed > threshold.  Tiles: `tiles` if given, else
     plan(shape, cores, halo); cores="auto" lets the autotuner measure the
-    candidate core sizes first.  mode: "core" or "blend" stitching."""
+    candidate core sizes first.  mode: "core" or "blend" stitching.
+
+    distributed=True shards the tiles over the ranks of the initialised
+    torch.distributed process group (one process per GPU, `device` its own):
+    rank r evolves lpt_shards(tiles, world)[r] with no collective during the
+    evolution, then every rank sends its evolved tiles to rank 0 (host
+    tensors with the gloo backend, device tensors with NCCL), which stitches
+    and returns the volume; the other ranks return None.  Every rank must
+    pass the same volume and parameters; with cores="auto" rank 0's choice
+    is broadcast."""
     import torch
 
     device = torch.device(device)
     shape = tuple(int(s) for s in image.shape)
     if tuple(seed.shape) != shape:
         raise ValueError(f"image {shape} and seed {tuple(seed.shape)} differ in shape")
+    rank, world = 0, 1
+    if distributed:
+        import torch.distributed as dist
+
+        if not dist.is_initialized():
+            raise RuntimeError("distributed=True needs an initialised torch.distributed process group")
+        rank, world = dist.get_rank(), dist.get_world_size()
     if tiles is None and cores == "auto":
         from .autotune import tune_cores
 
         dt = "u8" if str(image.dtype) in ("uint8", "torch.uint8") else "f32"
-        cores = tune_cores(shape, params, halo, dt, device=device).cores
+        if rank == 0:
+            cores = tune_cores(shape, params, halo, dt, device=device).cores
+        if world > 1:
+            box = [cores]
+            dist.broadcast_object_list(box, src=0)
+            cores = box[0]
     tiles = list(tiles) if tiles is not None else plan(shape, cores, halo)
+    shards = lpt_shards(tiles, world)
+    mine = shards[rank]
     if max_chunk_voxels is None:
         free, _ = torch.cuda.mem_get_info(device)
         reserve = 4 * (np.prod(shape) + sum(t.voxels for t in tiles))  # output + evolved tiles
         max_chunk_voxels = max(int((free - reserve) * 0.8) // _BYTES_PER_VOXEL, max(t.voxels for t in tiles))
-    groups = chunk_tiles(tiles, max_chunk_voxels)
-    ws_voxels = max(sum(tiles[i].voxels for i in g) for g in groups)
-    ws_tiles = max(len(tiles), max(len(g) for g in groups))
+    local = [tiles[i] for i in mine]
+    groups = [[mine[j] for j in g] for g in chunk_tiles(local, max_chunk_voxels)] if mine else []
+    ws_voxels = max([sum(tiles[i].voxels for i in g) for g in groups] + [1])
+    ws_tiles = max([len(tiles)] + [len(g) for g in groups])
     parts: List = [None] * len(tiles)
     with torch.cuda.device(device), Workspace(ws_voxels, ws_tiles) as ws:
         for g in groups:
@@ -98,9 +123,32 @@ def segment(image, seed, params: Params, iters: int, cores=256, halo: int = 32, 
                 parts[i] = phi
             ws.evolve_batched(pairs, params, iters)
             ws.check()
+        if world > 1:
+            _gather_tiles(parts, tiles, shards, rank, device)
+            if rank != 0:
+                return None
         out = reassemble_device(ws, tiles, parts, shape, mode)
         ws.check()
     return out
+
+
+def _gather_tiles(parts, tiles, shards, rank, device):
+    """Every rank's evolved tiles into rank 0's `parts`, in shard order, by
+    point-to-point sends (host tensors with gloo, device tensors with NCCL)."""
+    import torch
+    import torch.distributed as dist
+
+    on_host = dist.get_backend() == "gloo"
+    if rank != 0:
+        for i in shards[rank]:
+            t = parts[i]
+            dist.send(t.cpu() if on_host else t.contiguous(), dst=0)
+        return
+    for src in range(1, len(shards)):
+        for i in shards[src]:
+            buf = torch.empty(tiles[i].shape, dtype=torch.float32, device="cpu" if on_host else device)
+            dist.recv(buf, src=src)
+            parts[i] = buf.to(device) if on_host else buf
 
 
 def main(argv=None):

@@ -326,3 +326,50 @@ def test_launch_shape_autotuner_picks_the_fastest():
 def test_launch_shape_override_rejects_bad_values_without_device(rsflib):
     # a null workspace is rejected before any device work
     assert rsflib.rsf_workspace_set_launch_shape(None, 0, 0, -1) == 1
+
+
+def _gather_worker(rank, world, port, q):
+    import os
+
+    import torch
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from rsf_gb300 import driver, tiling
+
+    tiles = tiling.plan((20, 30, 26), 10, 3)
+    shards = tiling.lpt_shards(tiles, world)
+    parts = [None] * len(tiles)
+    for i in shards[rank]:
+        parts[i] = torch.full(tiles[i].shape, float(i))
+    driver._gather_tiles(parts, tiles, shards, rank, "cpu")
+    if rank == 0:
+        ok = all(p is not None and p.shape == tiles[i].shape and bool((p == i).all()) for i, p in enumerate(parts))
+        q.put((rank, ok, len(tiles)))
+    else:
+        q.put((rank, True, len(tiles)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_tile_gather_on_host():
+    """The sharded driver's gather: every rank's evolved tiles reach rank 0
+    in place, over gloo (the evolution itself needs no exchange)."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_gather_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][1] and res[0][2] == 2 * 3 * 3
