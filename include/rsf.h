@@ -241,6 +241,26 @@ rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *
                             const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
                             int64_t W, int64_t H, int64_t L, void *stream);
 
+/* One volume of an adjoint batch (rsf_step_adjoint_batched): the arguments
+ * of rsf_step_adjoint for that volume. */
+typedef struct {
+    const float *phi;        /* state before the step, W*H*L float32, device */
+    const void *image;       /* W*H*L image of the batch's dtype */
+    const float *phi_bar_in; /* dL/dphi' */
+    float *phi_bar_out;      /* dL/dphi (written) */
+    int64_t W, H, L;
+} rsf_adjoint_subvol;
+
+/* rsf_step_adjoint for n volumes that share the step parameters, as one
+ * launch sequence over the batch (the table of rsf_evolve_batched's kind).
+ * param_grads (device doubles, may be NULL) receives the parameter
+ * gradients summed over the batch.  Each phi_bar_out must be disjoint from
+ * every input and from the other outputs.  The workspace must hold the
+ * batch's total voxels and n sub-volumes. */
+rsf_status rsf_step_adjoint_batched(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype,
+                                    const rsf_adjoint_subvol *subvols, int32_t n, double *param_grads,
+                                    void *stream);
+
 /* Stitches a grid of evolved sub-volumes into `out` (W*H*L float32, device),
  * the step of the reference's missing reassemble.py (README.md:9) and of
  * interpolating_volumes.py:10-40.  Core boundaries core_x[0..nx] (0 .. W),

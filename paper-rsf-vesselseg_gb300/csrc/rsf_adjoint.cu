@@ -1,4 +1,5 @@
-// rsf_adjoint.cu -- reverse-mode derivative of one RSF step.
+// rsf_adjoint.cu -- reverse-mode derivative of one RSF step, for a batch of
+// volumes that share the step parameters.
 //
 // The forward step (CUDA_RSF/main.cpp:233-300, kernel.cu) maps phi to
 //   phi' = phi + dt * ( -delta(phi) * data + nu * delta(phi) * kappa + mu * (Lap - kappa) )
@@ -28,9 +29,22 @@
 // adjoint); transposed blur z, y, x (the x kernel forms H_bar); gradients and
 // unit normals; the pointwise terms with the parameter sums; the stencil
 // adjoint w; the final D^T gather.  The blurs along y and z compute several
-// consecutive outputs per thread; the last three kernels run on 3-D grids,
-// the others are grid-stride loops.  Scratch comes from the workspace pools;
-// the layout is given in launch_step_adjoint.
+// consecutive outputs per thread; the last three kernels run on blocks of
+// 32 x 8 voxels, the others on one item per thread.  Every kernel covers the
+// whole batch in one launch: a block finds its volume in a block prefix
+// array (one per kernel) and its tile within the volume.  For 21, 29 and 35
+// taps the caller replaces the first four kernels by the forward step's
+// streaming x- and y-passes and the z-pass's adjoint variant
+// (zpass_adjoint_kernel), which leave the same fields in xs.
+//
+// Scratch per volume (N = W H L; slices of the workspace pools of 1, 4 and
+// 4 floats per voxel):
+//   phi2 : H (blur input), later H_bar
+//   xs   : blur-x fields (4 Wv H L), then [0, 2N) the valid-layout adjoint pair
+//          and [2N, 4N) e_out, e_in (kappa_bar over e_out); then g_x, g_y in
+//          [0, 2N), later w_x, w_y
+//   ys   : blur-y fields (4 Wv Hv L), then the z-transposed pair [0, 2N), the
+//          y-transposed pair at 2N; later g_z (then w_z), n_x, n_y, n_z
 #include <cuda_runtime.h>
 
 #include "rsf_arith.cuh"
@@ -44,30 +58,50 @@ constexpr int kThreads = 256;
 struct AdjConst {
     float taps[MAXK];
     int k, r;
-    int W, H, L;
-    int Wv, Hv, Lv;  // valid blur extents; all > 0 or all 0
     float eps, dt, mu, nu, l1, l2;
     int boundary;    // 0 reference (x = 0 reads the previous linear element), 1 clamp
     int img_f32;
+    int nvol;
 };
 
 __device__ __forceinline__ float img_at(const void *img, long long i, int f32) {
     return f32 ? static_cast<const float *>(img)[i] : (float)static_cast<const unsigned char *>(img)[i];
 }
 
-__device__ __forceinline__ long long grid_start() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ long long grid_step() { return (long long)gridDim.x * blockDim.x; }
+// The volume of this block (binary search of the kernel's block prefix
+// array) and the block's index within it.  Kernels copy their volume's
+// descriptor by value, so that their stores cannot alias it and its fields
+// are loaded once.
+struct BlockVol {
+    int v;
+    long long t;
+};
+__device__ __forceinline__ BlockVol block_vol(const int *__restrict__ pre, int n) {
+    const int b = blockIdx.x;
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(pre + mid) <= b) lo = mid;
+        else hi = mid;
+    }
+    return {lo, (long long)(b - __ldg(pre + lo))};
+}
 
-// The stencil kernels run on 3-D grids of 32 x 8 blocks (x fastest, one z
-// plane per blockIdx.z), so voxel coordinates need no 64-bit division.
+// The stencil kernels run on blocks of 32 x 8 voxels of one z plane (w,
+// gather) or of kPointZ planes (pointwise terms).
 constexpr int kBX = 32, kBY = 8;
+constexpr int kPointZ = 16;
+
+struct Geo {
+    int W, H, L, boundary;
+};
 
 // Right and left linear indices of the central difference at voxel i.
-__device__ __forceinline__ void nb_x(const AdjConst &c, long long i, int x, long long &r, long long &l) {
-    r = x + 1 < c.W ? i + 1 : i;
+__device__ __forceinline__ void nb_x(const Geo &g, long long i, int x, long long &r, long long &l) {
+    r = x + 1 < g.W ? i + 1 : i;
     if (x > 0) l = i - 1;
-    else l = c.boundary == 0 ? (i > 0 ? i - 1 : 0) : i;
-    if (x == c.W - 1) l = i - 1;
+    else l = g.boundary == 0 ? (i > 0 ? i - 1 : 0) : i;
+    if (x == g.W - 1) l = i - 1;
 }
 // y and z: (f[1] - f[0]) / 2 at 0, (f[n-1] - f[n-2]) / 2 at n - 1 (n >= 2).
 __device__ __forceinline__ void nb_axis(long long i, int q, int n, long long stride, long long &r, long long &l) {
@@ -77,19 +111,14 @@ __device__ __forceinline__ void nb_axis(long long i, int q, int n, long long str
     l = i + (long long)(ql - q) * stride;
 }
 
-__device__ __forceinline__ float diff_x_at(const AdjConst &c, const float *f, long long m) {
+__device__ __forceinline__ float diff_x_at(const Geo &g, const float *f, long long m, int x) {
     long long r, l;
-    nb_x(c, m, (int)(m % c.W), r, l);
+    nb_x(g, m, x, r, l);
     return 0.5f * (f[r] - f[l]);
 }
-__device__ __forceinline__ float diff_y_at(const AdjConst &c, const float *f, long long m, int y) {
+__device__ __forceinline__ float diff_axis_at(const float *f, long long m, int q, int n, long long stride) {
     long long r, l;
-    nb_axis(m, y, c.H, c.W, r, l);
-    return 0.5f * (f[r] - f[l]);
-}
-__device__ __forceinline__ float diff_z_at(const AdjConst &c, const float *f, long long m, int z) {
-    long long r, l;
-    nb_axis(m, z, c.L, (long long)c.W * c.H, r, l);
+    nb_axis(m, q, n, stride, r, l);
     return 0.5f * (f[r] - f[l]);
 }
 
@@ -99,16 +128,16 @@ __device__ __forceinline__ float diff_z_at(const AdjConst &c, const float *f, lo
 // row's start and vice versa.  Branch-free: an out-of-range candidate is
 // read as j itself with coefficient 0, so that all loads issue together.
 template <class V>
-__device__ __forceinline__ float dT_x(const AdjConst &c, long long j, int x, long long N, V v) {
+__device__ __forceinline__ float dT_x(const Geo &g, long long j, int x, long long N, V v) {
     float acc = 0.0f;
 #pragma unroll
     for (int d = -1; d <= 1; d++) {
         const long long m0 = j + d;
         const bool in = m0 >= 0 && m0 < N;
         const long long m = in ? m0 : j;
-        const int mx = d == 0 ? x : d < 0 ? (x > 0 ? x - 1 : c.W - 1) : (x + 1 < c.W ? x + 1 : 0);
+        const int mx = d == 0 ? x : d < 0 ? (x > 0 ? x - 1 : g.W - 1) : (x + 1 < g.W ? x + 1 : 0);
         long long r, l;
-        nb_x(c, m, mx, r, l);
+        nb_x(g, m, mx, r, l);
         const float coef = in ? (r == j ? 0.5f : 0.0f) - (l == j ? 0.5f : 0.0f) : 0.0f;
         acc = fmaf(coef, v(m), acc);
     }
@@ -136,33 +165,44 @@ __device__ __forceinline__ float dirac_fast(float phi, float eps) {
     return __fdividef(0.318309886183790672f * eps, fmaf(phi, phi, eps * eps));
 }
 
-__global__ void adj_heaviside(AdjConst c, const float *phi, float *h, long long N) {
-    for (long long i = grid_start(); i < N; i += grid_step()) h[i] = heaviside<Arith::Portable>(phi[i], c.eps);
+__device__ __forceinline__ long long nvox(const AdjVol &a) { return (long long)a.W * a.H * a.L; }
+__device__ __forceinline__ long long item(const BlockVol &bv) { return bv.t * kThreads + threadIdx.x; }
+
+__global__ void __launch_bounds__(kThreads) adj_heaviside(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long i = item(bv);
+    if (i < nvox(a)) a.phi2[i] = heaviside<Arith::Portable>(a.phi[i], c.eps);
 }
 
-// Valid correlation along x of (I H, H, I (1-H), 1-H): (Wv, H, L) per field.
-__global__ void adj_blur_x(AdjConst c, const float *h, const void *img, float *out) {
-    const long long n = (long long)c.Wv * c.H * c.L;
-    for (long long o = grid_start(); o < n; o += grid_step()) {
-        const int xv = (int)(o % c.Wv);
-        const long long row = o / c.Wv;  // z * H + y
-        const long long base = row * c.W + xv;
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-        for (int t = 0; t < c.k; t++) {
-            const float hv = h[base + t];
-            const float I = img_at(img, base + t, c.img_f32);
-            const float hi = 1.0f - hv;
-            const float g = c.taps[t];
-            a0 = fmaf(I * hv, g, a0);
-            a1 = fmaf(hv, g, a1);
-            a2 = fmaf(I * hi, g, a2);
-            a3 = fmaf(hi, g, a3);
-        }
-        out[o] = a0;
-        out[n + o] = a1;
-        out[2 * n + o] = a2;
-        out[3 * n + o] = a3;
+// Valid correlation along x of (I H, H, I (1-H), 1-H): (Wv, H, L) per field,
+// from H in phi2 to xs.
+__global__ void __launch_bounds__(kThreads) adj_blur_x(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long n = (long long)a.Wv * a.H * a.L;
+    const long long o = item(bv);
+    if (o >= n) return;
+    const int xv = (int)(o % a.Wv);
+    const long long row = o / a.Wv;  // z * H + y
+    const long long base = row * a.W + xv;
+    const float *h = a.phi2;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    for (int t = 0; t < c.k; t++) {
+        const float hv = h[base + t];
+        const float I = img_at(a.img, base + t, c.img_f32);
+        const float hi = 1.0f - hv;
+        const float g = c.taps[t];
+        a0 = fmaf(I * hv, g, a0);
+        a1 = fmaf(hv, g, a1);
+        a2 = fmaf(I * hi, g, a2);
+        a3 = fmaf(hi, g, a3);
     }
+    float *out = a.xs;
+    out[o] = a0;
+    out[n + o] = a1;
+    out[2 * n + o] = a2;
+    out[3 * n + o] = a3;
 }
 
 // Correlation of NB consecutive outputs start .. start+NB-1 along a strided
@@ -189,139 +229,170 @@ __device__ __forceinline__ void corr_block(const AdjConst &c, const float *__res
 constexpr int kNB = 8;   // outputs per thread along z
 constexpr int kNBy = 4;  // outputs per thread along y (shorter columns keep more threads in flight)
 
-// Valid correlation along y: (Wv, H, L) -> (Wv, Hv, L), four fields.
-__global__ void adj_blur_y(AdjConst c, const float *in, float *out) {
-    const long long nin = (long long)c.Wv * c.H * c.L, n = (long long)c.Wv * c.Hv * c.L;
-    const int nyb = (c.Hv + kNBy - 1) / kNBy;
-    const long long cols = (long long)c.Wv * nyb * c.L;
-    for (long long q = grid_start(); q < cols; q += grid_step()) {
-        const int xv = (int)(q % c.Wv);
-        const long long t1 = q / c.Wv;
-        const int y0 = (int)(t1 % nyb) * kNBy;
-        const int z = (int)(t1 / nyb);
-        for (int f = 0; f < 4; f++) {
-            float acc[kNBy];
-            corr_block<kNBy, false>(c, in + f * nin + (long long)z * c.H * c.Wv + xv, c.Wv, y0, c.H, acc);
+// Valid correlation along y: xs (Wv, H, L) -> ys (Wv, Hv, L), four fields.
+__global__ void __launch_bounds__(kThreads) adj_blur_y(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long nin = (long long)a.Wv * a.H * a.L, n = (long long)a.Wv * a.Hv * a.L;
+    const int nyb = (a.Hv + kNBy - 1) / kNBy;
+    const long long q = item(bv);
+    if (q >= (long long)a.Wv * nyb * a.L) return;
+    const int xv = (int)(q % a.Wv);
+    const long long t1 = q / a.Wv;
+    const int y0 = (int)(t1 % nyb) * kNBy;
+    const int z = (int)(t1 / nyb);
+    for (int f = 0; f < 4; f++) {
+        float acc[kNBy];
+        corr_block<kNBy, false>(c, a.xs + f * nin + (long long)z * a.H * a.Wv + xv, a.Wv, y0, a.H, acc);
 #pragma unroll
-            for (int m = 0; m < kNBy; ++m)
-                if (y0 + m < c.Hv) out[f * n + ((long long)z * c.Hv + y0 + m) * c.Wv + xv] = acc[m];
-        }
+        for (int m = 0; m < kNBy; ++m)
+            if (y0 + m < a.Hv) a.ys[f * n + ((long long)z * a.Hv + y0 + m) * a.Wv + xv] = acc[m];
     }
 }
 
 // Valid correlation along z, then the data-term adjoint at each valid voxel:
-// writes (B1_bar - B3_bar, B2_bar - B4_bar) in the valid layout and e_out,
-// e_in at the full-volume index.
-__global__ void adj_blur_z_data(AdjConst c, const float *in, const float *phi, const void *img, const float *u,
-                                float *pq, float *eo_out, float *ei_out) {
-    const long long nin = (long long)c.Wv * c.Hv * c.L, n = (long long)c.Wv * c.Hv * c.Lv;
-    const long long plane = (long long)c.Wv * c.Hv;
-    const int nzb = (c.Lv + kNB - 1) / kNB;
-    const long long cols = plane * nzb;
-    for (long long q = grid_start(); q < cols; q += grid_step()) {
-        const long long pxy = q % plane;
-        const int z0 = (int)(q / plane) * kNB;
-        const int xv = (int)(pxy % c.Wv), yv = (int)(pxy / c.Wv);
-        float B[4][kNB];
-        for (int f = 0; f < 4; f++) corr_block<kNB, false>(c, in + f * nin + pxy, plane, z0, c.L, B[f]);
+// writes (B1_bar - B3_bar, B2_bar - B4_bar) in the valid layout to xs and
+// e_out, e_in at the full-volume index to xs + 2N, xs + 3N.
+__global__ void __launch_bounds__(kThreads) adj_blur_z_data(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long nin = (long long)a.Wv * a.Hv * a.L, n = (long long)a.Wv * a.Hv * a.Lv;
+    const long long plane = (long long)a.Wv * a.Hv;
+    const int nzb = (a.Lv + kNB - 1) / kNB;
+    const long long q = item(bv);
+    if (q >= plane * nzb) return;
+    const long long pxy = q % plane;
+    const int z0 = (int)(q / plane) * kNB;
+    const int xv = (int)(pxy % a.Wv), yv = (int)(pxy / a.Wv);
+    float B[4][kNB];
+    for (int f = 0; f < 4; f++) corr_block<kNB, false>(c, a.ys + f * nin + pxy, plane, z0, a.L, B[f]);
+    float *pq = a.xs, *eo_out = a.xs + 2 * N, *ei_out = a.xs + 3 * N;
 #pragma unroll
-        for (int m = 0; m < kNB; ++m) {
-            const int zv = z0 + m;
-            if (zv >= c.Lv) break;
-            const long long o = (long long)zv * plane + pxy;
-            const long long i = ((long long)(zv + c.r) * c.H + (yv + c.r)) * c.W + xv + c.r;
-            const float I = img_at(img, i, c.img_f32);
-            const float rb1 = __frcp_rn(B[1][m]), rb3 = __frcp_rn(B[3][m]);
-            const float fo = B[0][m] * rb1, fi = B[2][m] * rb3;
-            const float dfo = I - fo, dfi = I - fi;
-            eo_out[i] = dfo * dfo;
-            ei_out[i] = dfi * dfi;
-            const float delta = dirac_fast(phi[i], c.eps);
-            const float data_bar = -u[i] * c.dt * delta;
-            const float fo_bar = -2.0f * dfo * (c.l1 * data_bar);
-            const float fi_bar = -2.0f * dfi * (-c.l2 * data_bar);
-            const float b1 = fo_bar * rb1, b2 = -fo_bar * fo * rb1;
-            const float b3 = fi_bar * rb3, b4 = -fi_bar * fi * rb3;
-            pq[o] = b1 - b3;
-            pq[n + o] = b2 - b4;
-        }
+    for (int m = 0; m < kNB; ++m) {
+        const int zv = z0 + m;
+        if (zv >= a.Lv) break;
+        const long long o = (long long)zv * plane + pxy;
+        const long long i = ((long long)(zv + c.r) * a.H + (yv + c.r)) * a.W + xv + c.r;
+        const float I = img_at(a.img, i, c.img_f32);
+        const float rb1 = __frcp_rn(B[1][m]), rb3 = __frcp_rn(B[3][m]);
+        const float fo = B[0][m] * rb1, fi = B[2][m] * rb3;
+        const float dfo = I - fo, dfi = I - fi;
+        eo_out[i] = dfo * dfo;
+        ei_out[i] = dfi * dfi;
+        const float delta = dirac_fast(a.phi[i], c.eps);
+        const float data_bar = -a.u[i] * c.dt * delta;
+        const float fo_bar = -2.0f * dfo * (c.l1 * data_bar);
+        const float fi_bar = -2.0f * dfi * (-c.l2 * data_bar);
+        const float b1 = fo_bar * rb1, b2 = -fo_bar * fo * rb1;
+        const float b3 = fi_bar * rb3, b4 = -fi_bar * fi * rb3;
+        pq[o] = b1 - b3;
+        pq[n + o] = b2 - b4;
     }
 }
 
-// Transposed (full) correlation along z: (Wv, Hv, Lv) -> (Wv, Hv, L), two fields.
-__global__ void adj_blurT_z(AdjConst c, const float *in, float *out) {
-    const long long nin = (long long)c.Wv * c.Hv * c.Lv, n = (long long)c.Wv * c.Hv * c.L;
-    const long long plane = (long long)c.Wv * c.Hv;
-    const int nzb = (c.L + kNB - 1) / kNB;
-    const long long cols = plane * nzb;
-    for (long long q = grid_start(); q < cols; q += grid_step()) {
-        const long long pxy = q % plane;
-        const int z0 = (int)(q / plane) * kNB;
-        for (int f = 0; f < 2; f++) {
-            float acc[kNB];
-            corr_block<kNB, true>(c, in + f * nin + pxy, plane, z0, c.Lv, acc);
+// Transposed (full) correlation along z: xs (Wv, Hv, Lv) -> ys (Wv, Hv, L), two fields.
+__global__ void __launch_bounds__(kThreads) adj_blurT_z(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long nin = (long long)a.Wv * a.Hv * a.Lv, n = (long long)a.Wv * a.Hv * a.L;
+    const long long plane = (long long)a.Wv * a.Hv;
+    const int nzb = (a.L + kNB - 1) / kNB;
+    const long long q = item(bv);
+    if (q >= plane * nzb) return;
+    const long long pxy = q % plane;
+    const int z0 = (int)(q / plane) * kNB;
+    for (int f = 0; f < 2; f++) {
+        float acc[kNB];
+        corr_block<kNB, true>(c, a.xs + f * nin + pxy, plane, z0, a.Lv, acc);
 #pragma unroll
-            for (int m = 0; m < kNB; ++m)
-                if (z0 + m < c.L) out[f * n + (long long)(z0 + m) * plane + pxy] = acc[m];
-        }
+        for (int m = 0; m < kNB; ++m)
+            if (z0 + m < a.L) a.ys[f * n + (long long)(z0 + m) * plane + pxy] = acc[m];
     }
 }
 
-// Transposed correlation along y: (Wv, Hv, L) -> (Wv, H, L).
-__global__ void adj_blurT_y(AdjConst c, const float *in, float *out) {
-    const long long nin = (long long)c.Wv * c.Hv * c.L, n = (long long)c.Wv * c.H * c.L;
-    const int nyb = (c.H + kNBy - 1) / kNBy;
-    const long long cols = (long long)c.Wv * nyb * c.L;
-    for (long long q = grid_start(); q < cols; q += grid_step()) {
-        const int xv = (int)(q % c.Wv);
-        const long long t1 = q / c.Wv;
-        const int y0 = (int)(t1 % nyb) * kNBy;
-        const int z = (int)(t1 / nyb);
-        for (int f = 0; f < 2; f++) {
-            float acc[kNBy];
-            corr_block<kNBy, true>(c, in + f * nin + (long long)z * c.Hv * c.Wv + xv, c.Wv, y0, c.Hv, acc);
+// Transposed correlation along y: ys (Wv, Hv, L) -> ys + 2N (Wv, H, L).
+__global__ void __launch_bounds__(kThreads) adj_blurT_y(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long nin = (long long)a.Wv * a.Hv * a.L, n = (long long)a.Wv * a.H * a.L;
+    const int nyb = (a.H + kNBy - 1) / kNBy;
+    const long long q = item(bv);
+    if (q >= (long long)a.Wv * nyb * a.L) return;
+    const int xv = (int)(q % a.Wv);
+    const long long t1 = q / a.Wv;
+    const int y0 = (int)(t1 % nyb) * kNBy;
+    const int z = (int)(t1 / nyb);
+    float *out = a.ys + 2 * nvox(a);
+    for (int f = 0; f < 2; f++) {
+        float acc[kNBy];
+        corr_block<kNBy, true>(c, a.ys + f * nin + (long long)z * a.Hv * a.Wv + xv, a.Wv, y0, a.Hv, acc);
 #pragma unroll
-            for (int m = 0; m < kNBy; ++m)
-                if (y0 + m < c.H) out[f * n + ((long long)z * c.H + y0 + m) * c.Wv + xv] = acc[m];
-        }
+        for (int m = 0; m < kNBy; ++m)
+            if (y0 + m < a.H) out[f * n + ((long long)z * a.H + y0 + m) * a.Wv + xv] = acc[m];
     }
 }
 
-// Transposed correlation along x and H_bar = I * P~ + Q~ over the volume.
-__global__ void adj_blurT_x_hbar(AdjConst c, const float *in, const void *img, float *hbar) {
-    const long long nin = (long long)c.Wv * c.H * c.L, N = (long long)c.W * c.H * c.L;
-    for (long long i = grid_start(); i < N; i += grid_step()) {
-        const int x = (int)(i % c.W);
-        const long long row = i / c.W;
-        const int a0 = max(0, x - c.Wv + 1), a1 = min(c.k - 1, x);
-        float p = 0.0f, q = 0.0f;
-        for (int t = a0; t <= a1; t++) {
-            const long long s = row * c.Wv + (x - t);
-            p = fmaf(in[s], c.taps[t], p);
-            q = fmaf(in[nin + s], c.taps[t], q);
-        }
-        hbar[i] = fmaf(img_at(img, i, c.img_f32), p, q);
+// Transposed correlation along x and H_bar = I * P~ + Q~ over the volume,
+// into phi2 (0 for a volume without a valid region).
+__global__ void __launch_bounds__(kThreads) adj_blurT_x_hbar(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long nin = (long long)a.Wv * a.H * a.L;
+    const long long i = item(bv);
+    if (i >= N) return;
+    if (a.Wv == 0) {
+        a.phi2[i] = 0.0f;
+        return;
     }
+    const float *in = a.ys + 2 * N;
+    const int x = (int)(i % a.W);
+    const long long row = i / a.W;
+    const int a0 = max(0, x - a.Wv + 1), a1 = min(c.k - 1, x);
+    float p = 0.0f, q = 0.0f;
+    for (int t = a0; t <= a1; t++) {
+        const long long s = row * a.Wv + (x - t);
+        p = fmaf(in[s], c.taps[t], p);
+        q = fmaf(in[nin + s], c.taps[t], q);
+    }
+    a.phi2[i] = fmaf(img_at(a.img, i, c.img_f32), p, q);
 }
 
 // Gradient g = D phi and unit normals n = g / (|g| + 1e-6), stored so that
-// the stencil adjoint reads them at its neighbours instead of recomputing.
-__global__ void adj_normals(AdjConst c, const float *phi, float *gxo, float *gyo, float *gzo, float *nx, float *ny,
-                            float *nz) {
-    const long long N = (long long)c.W * c.H * c.L;
-    for (long long i = grid_start(); i < N; i += grid_step()) {
-        const long long t1 = i / c.W;
-        const int y = (int)(t1 % c.H);
-        const int z = (int)(t1 / c.H);
-        const float gx = diff_x_at(c, phi, i), gy = diff_y_at(c, phi, i, y), gz = diff_z_at(c, phi, i, z);
-        const float rs = __frcp_rn(sqrtf(gx * gx + gy * gy + gz * gz) + 1e-6f);
-        gxo[i] = gx;
-        gyo[i] = gy;
-        gzo[i] = gz;
-        nx[i] = gx * rs;
-        ny[i] = gy * rs;
-        nz[i] = gz * rs;
-    }
+// the stencil adjoint reads them at its neighbours instead of recomputing:
+// g_x, g_y to xs, xs + N; g_z, n_x, n_y, n_z to ys .. ys + 3N.
+__global__ void __launch_bounds__(kThreads) adj_normals(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long i = item(bv);
+    if (i >= N) return;
+    const Geo g = {a.W, a.H, a.L, c.boundary};
+    const int x = (int)(i % a.W);
+    const long long t1 = i / a.W;
+    const int y = (int)(t1 % a.H);
+    const int z = (int)(t1 / a.H);
+    const float gx = diff_x_at(g, a.phi, i, x), gy = diff_axis_at(a.phi, i, y, a.H, a.W),
+                gz = diff_axis_at(a.phi, i, z, a.L, (long long)a.W * a.H);
+    const float rs = __frcp_rn(sqrtf(gx * gx + gy * gy + gz * gz) + 1e-6f);
+    a.xs[i] = gx;
+    a.xs[N + i] = gy;
+    a.ys[i] = gz;
+    a.ys[N + i] = gx * rs;
+    a.ys[2 * N + i] = gy * rs;
+    a.ys[3 * N + i] = gz * rs;
+}
+
+// The block's 32 x 8 column: x, y of this thread and the first z plane.
+struct Col {
+    int x, y, z0;
+};
+__device__ __forceinline__ Col col_of(const AdjVol &a, long long t, int zdepth) {
+    const int nbx = (a.W + kBX - 1) / kBX, nby = (a.H + kBY - 1) / kBY;
+    const long long t1 = t / nbx;
+    return {(int)(t % nbx) * kBX + (int)threadIdx.x, (int)(t1 % nby) * kBY + (int)threadIdx.y,
+            (int)(t1 / nby) * zdepth};
 }
 
 // Pointwise terms and parameter sums:
@@ -330,30 +401,37 @@ __global__ void adj_normals(AdjConst c, const float *phi, float *gxo, float *gyo
 // A block covers a 32 x 8 column of kPointZ planes; the parameter sums are
 // reduced in the block and added with one double atomic per parameter and
 // block (the same four addresses for every block, so their number matters).
-constexpr int kPointZ = 16;
-__global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const float *phi, const void *img,
-                                                       const float *u, const float *gxa, const float *gya,
-                                                       const float *gza, const float *nx, const float *ny,
-                                                       const float *nz, const float *hbar, const float *eo_v,
-                                                       const float *ei_v, float *out, double *grads) {
-    const long long plane = (long long)c.W * c.H;
+// kappa_bar = u dt (nu delta - mu) is written over e_out (read first, by the
+// same thread) for adj_w.
+__global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
+                                                       double *grads) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long plane = (long long)a.W * a.H;
+    const Geo g = {a.W, a.H, a.L, c.boundary};
+    const float *gxa = a.xs, *gya = a.xs + N, *gza = a.ys;
+    const float *nx = a.ys + N, *ny = a.ys + 2 * N, *nz = a.ys + 3 * N;
+    float *eo_v = a.xs + 2 * N;
+    const float *ei_v = a.xs + 3 * N;
     float s_l1 = 0.0f, s_l2 = 0.0f, s_mu = 0.0f, s_nu = 0.0f;
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
-    const int z0 = blockIdx.z * kPointZ, z1 = min(z0 + kPointZ, c.L);
-    for (int z = z0; z < z1 && x < c.W && y < c.H; ++z) {
-        const long long i = ((long long)z * c.H + y) * c.W + x;
-        const float ph = phi[i], ui = u[i];
-        const float I = img_at(img, i, c.img_f32);
+    const Col cl = col_of(a, bv.t, kPointZ);
+    const int x = cl.x, y = cl.y;
+    const int z1 = min(cl.z0 + kPointZ, a.L);
+    for (int z = cl.z0; z < z1 && x < a.W && y < a.H; ++z) {
+        const long long i = ((long long)z * a.H + y) * a.W + x;
+        const float ph = a.phi[i], ui = a.u[i];
+        const float I = img_at(a.img, i, c.img_f32);
         const float delta = dirac_fast(ph, c.eps);
         const float ddelta = __fdividef(-2.0f * ph * delta, fmaf(ph, ph, c.eps * c.eps));
         long long rx, lx, ry, ly, rz, lz;
-        nb_x(c, i, x, rx, lx);
-        nb_axis(i, y, c.H, c.W, ry, ly);
-        nb_axis(i, z, c.L, plane, rz, lz);
+        nb_x(g, i, x, rx, lx);
+        nb_axis(i, y, a.H, a.W, ry, ly);
+        nb_axis(i, z, a.L, plane, rz, lz);
         const float kap = 0.5f * (nx[rx] - nx[lx]) + 0.5f * (ny[ry] - ny[ly]) + 0.5f * (nz[rz] - nz[lz]);
         const float lap = 0.5f * (gxa[rx] - gxa[lx]) + 0.5f * (gya[ry] - gya[ly]) + 0.5f * (gza[rz] - gza[lz]);
-        const bool valid = c.Wv > 0 && x >= c.r && x < c.r + c.Wv && y >= c.r && y < c.r + c.Hv && z >= c.r &&
-                           z < c.r + c.Lv;
+        const bool valid = a.Wv > 0 && x >= c.r && x < c.r + a.Wv && y >= c.r && y < c.r + a.Hv && z >= c.r &&
+                           z < c.r + a.Lv;
         float eo, ei;
         if (valid) {
             eo = eo_v[i];
@@ -362,8 +440,9 @@ __global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const float *
             eo = ei = (I - 1.0f) * (I - 1.0f);
         }
         const float data = c.l1 * eo - c.l2 * ei;
-        out[i] = ui + delta * hbar[i] + ddelta * ui * c.dt * (c.nu * kap - data);
+        a.out[i] = ui + delta * a.phi2[i] + ddelta * ui * c.dt * (c.nu * kap - data);
         const float ud = ui * c.dt, udd = ud * delta;
+        eo_v[i] = ud * (c.nu * delta - c.mu);
         s_l1 = fmaf(-udd, eo, s_l1);
         s_l2 = fmaf(udd, ei, s_l2);
         s_mu = fmaf(ud, lap - kap, s_mu);
@@ -394,114 +473,118 @@ __global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const float *
 }
 
 // Stencil adjoint: w_a = D_a^T Lap_bar + (n_bar_a - (n_bar . n) g_a/|g|) / (|g| + 1e-6)
-// with n_bar = D^T kappa_bar, to be gathered by D_a^T.  Runs after adj_point,
-// which has read H_bar, e_out and e_in: w is written over them.
-__global__ void adj_w(AdjConst c, const float *phi, const float *u, const float *gxa, const float *gya,
-                      const float *gza, const float *nx, const float *ny, const float *nz, float *wx, float *wy,
-                      float *wz) {
-    const long long N = (long long)c.W * c.H * c.L;
-    const long long plane = (long long)c.W * c.H;
-    auto kbar = [&](long long m) { return u[m] * c.dt * (c.nu * dirac_fast(phi[m], c.eps) - c.mu); };
+// with n_bar = D^T kappa_bar, to be gathered by D_a^T.  kappa_bar comes from
+// adj_point; Lap_bar = u dt mu.  Each thread reads g and n at its own voxel
+// only, so w is written over g in place.
+__global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long plane = (long long)a.W * a.H;
+    const Geo g = {a.W, a.H, a.L, c.boundary};
+    const float *kb = a.xs + 2 * N, *u = a.u;
+    auto kbar = [&](long long m) { return kb[m]; };
     auto lbar = [&](long long m) { return u[m] * c.dt * c.mu; };
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y, z = blockIdx.z;
-    if (x < c.W && y < c.H) {
-        const long long i = ((long long)z * c.H + y) * c.W + x;
+    const Col cl = col_of(a, bv.t, 1);
+    const int x = cl.x, y = cl.y, z = cl.z0;
+    if (x < a.W && y < a.H) {
+        float *gxa = a.xs, *gya = a.xs + N, *gza = a.ys;
+        const float *nx = a.ys + N, *ny = a.ys + 2 * N, *nz = a.ys + 3 * N;
+        const long long i = ((long long)z * a.H + y) * a.W + x;
         const float gx = gxa[i], gy = gya[i], gz = gza[i];
         const float mag = sqrtf(gx * gx + gy * gy + gz * gz);
         const float rs = __frcp_rn(mag + 1e-6f);
         const float inv_mag = mag > 0.0f ? __frcp_rn(mag) : 0.0f;
-        const float nbx = dT_x(c, i, x, N, kbar), nby = dT_axis(i, y, c.H, c.W, kbar),
-                    nbz = dT_axis(i, z, c.L, plane, kbar);
-        const float lbx = dT_x(c, i, x, N, lbar), lby = dT_axis(i, y, c.H, c.W, lbar),
-                    lbz = dT_axis(i, z, c.L, plane, lbar);
+        const float nbx = dT_x(g, i, x, N, kbar), nby = dT_axis(i, y, a.H, a.W, kbar),
+                    nbz = dT_axis(i, z, a.L, plane, kbar);
+        const float lbx = dT_x(g, i, x, N, lbar), lby = dT_axis(i, y, a.H, a.W, lbar),
+                    lbz = dT_axis(i, z, a.L, plane, lbar);
         const float ndot = nbx * nx[i] + nby * ny[i] + nbz * nz[i];
-        wx[i] = lbx + (nbx - ndot * gx * inv_mag) * rs;
-        wy[i] = lby + (nby - ndot * gy * inv_mag) * rs;
-        wz[i] = lbz + (nbz - ndot * gz * inv_mag) * rs;
+        gxa[i] = lbx + (nbx - ndot * gx * inv_mag) * rs;
+        gya[i] = lby + (nby - ndot * gy * inv_mag) * rs;
+        gza[i] = lbz + (nbz - ndot * gz * inv_mag) * rs;
     }
 }
 
 // out += sum_a D_a^T w_a; a non-finite result sets kFlagAdjointNonFinite.
-__global__ void adj_gather(AdjConst c, const float *wx, const float *wy, const float *wz, float *out,
-                           unsigned *flag) {
-    const long long N = (long long)c.W * c.H * c.L;
-    const long long plane = (long long)c.W * c.H;
+__global__ void __launch_bounds__(kBX * kBY) adj_gather(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
+                                                        unsigned *flag) {
+    const BlockVol bv = block_vol(pre, c.nvol);
+    const AdjVol a = vols[bv.v];
+    const long long N = nvox(a);
+    const long long plane = (long long)a.W * a.H;
+    const Geo g = {a.W, a.H, a.L, c.boundary};
+    const float *wx = a.xs, *wy = a.xs + N, *wz = a.ys;
     auto vx = [&](long long m) { return wx[m]; };
     auto vy = [&](long long m) { return wy[m]; };
     auto vz = [&](long long m) { return wz[m]; };
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y, z = blockIdx.z;
-    if (x < c.W && y < c.H) {
-        const long long i = ((long long)z * c.H + y) * c.W + x;
-        const float v = out[i] + (dT_x(c, i, x, N, vx) + dT_axis(i, y, c.H, c.W, vy) + dT_axis(i, z, c.L, plane, vz));
-        out[i] = v;
+    const Col cl = col_of(a, bv.t, 1);
+    const int x = cl.x, y = cl.y, z = cl.z0;
+    if (x < a.W && y < a.H) {
+        const long long i = ((long long)z * a.H + y) * a.W + x;
+        const float v = a.out[i] + (dT_x(g, i, x, N, vx) + dT_axis(i, y, a.H, a.W, vy) + dT_axis(i, z, a.L, plane, vz));
+        a.out[i] = v;
         if (!isfinite(v) && flag) atomicOr(flag, kFlagAdjointNonFinite);
     }
 }
 
-unsigned blocks_for(long long n) {
-    const long long b = (n + kThreads - 1) / kThreads, cap = 64LL * sm_count();
-    return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
-}
+long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
 
 }  // namespace
 
-// Scratch (N = W H L; the pools hold 1, 4 and 4 N floats):
-//   phi2 : H (blur input), later H_bar, then w_x
-//   xs   : blur-x fields (4 Wv H L), then [0, 2N) the valid-layout adjoint pair
-//          and [2N, 4N) e_out, e_in (later w_y, w_z); then g_x, g_y in [0, 2N)
-//   ys   : blur-y fields (4 Wv Hv L), then the z-transposed pair [0, 2N), the
-//          y-transposed pair at 2N; later g_z, n_x, n_y, n_z
-cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,
-                                int boundary, int img_f32, const float *phi, const void *img, const float *u,
-                                float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
-                                unsigned *flag, cudaStream_t st) {
+void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]) {
+    const long long N = (long long)v.W * v.H * v.L;
+    const bool valid = v.Wv > 0;
+    const long long bxy = cdiv(v.W, kBX) * cdiv(v.H, kBY);
+    long long t[NADJ] = {};
+    if (valid) {
+        if (!streamed) {
+            t[ADJ_H] = cdiv(N, kThreads);
+            t[ADJ_BX] = cdiv((long long)v.Wv * v.H * v.L, kThreads);
+            t[ADJ_BY] = cdiv((long long)v.Wv * cdiv(v.Hv, kNBy) * v.L, kThreads);
+            t[ADJ_BZ] = cdiv((long long)v.Wv * v.Hv * cdiv(v.Lv, kNB), kThreads);
+        }
+        t[ADJ_TZ] = cdiv((long long)v.Wv * v.Hv * cdiv(v.L, kNB), kThreads);
+        t[ADJ_TY] = cdiv((long long)v.Wv * cdiv(v.H, kNBy) * v.L, kThreads);
+    }
+    (void)k;
+    t[ADJ_TX] = cdiv(N, kThreads);
+    t[ADJ_NRM] = cdiv(N, kThreads);
+    t[ADJ_PT] = bxy * cdiv(v.L, kPointZ);
+    t[ADJ_W] = bxy * v.L;
+    t[ADJ_G] = bxy * v.L;
+    for (int j = 0; j < NADJ; j++) tiles[j] = t[j] > 0x7fffffffLL ? -1 : (int)t[j];
+}
+
+cudaError_t launch_step_adjoint(const float *taps, int k, const AdjScalars &s, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
+                                int n, const int *tot, double *grads, unsigned *flag, cudaStream_t st) {
     AdjConst c;
     for (int t = 0; t < MAXK; t++) c.taps[t] = t < k ? taps[t] : 0.0f;
     c.k = k;
     c.r = (k - 1) / 2;
-    c.W = W;
-    c.H = H;
-    c.L = L;
-    c.Wv = W - k + 1;
-    c.Hv = H - k + 1;
-    c.Lv = L - k + 1;
-    if (c.Wv <= 0 || c.Hv <= 0 || c.Lv <= 0) c.Wv = c.Hv = c.Lv = 0;
-    c.eps = eps;
-    c.dt = dt;
-    c.mu = mu;
-    c.nu = nu;
-    c.l1 = l1;
-    c.l2 = l2;
-    c.boundary = boundary;
-    c.img_f32 = img_f32;
-    const long long N = (long long)W * H * L;
-    float *hbar = phi2;
-    float *eo = xs + 2 * N, *ei = xs + 3 * N;
-    if (c.Wv > 0) {
-        const long long nx = (long long)c.Wv * H * L, ny = (long long)c.Wv * c.Hv * L;
-        const long long nz = (long long)c.Wv * c.Hv * c.Lv;
-        adj_heaviside<<<blocks_for(N), kThreads, 0, st>>>(c, phi, phi2, N);
-        adj_blur_x<<<blocks_for(nx), kThreads, 0, st>>>(c, phi2, img, xs);
-        const long long pl = (long long)c.Wv * c.Hv;
-        adj_blur_y<<<blocks_for((long long)c.Wv * L * ((c.Hv + kNBy - 1) / kNBy)), kThreads, 0, st>>>(c, xs, ys);
-        adj_blur_z_data<<<blocks_for(pl * ((c.Lv + kNB - 1) / kNB)), kThreads, 0, st>>>(c, ys, phi, img, u, xs,
-                                                                                          eo, ei);
-        adj_blurT_z<<<blocks_for(pl * ((L + kNB - 1) / kNB)), kThreads, 0, st>>>(c, xs, ys);
-        adj_blurT_y<<<blocks_for((long long)c.Wv * L * ((H + kNBy - 1) / kNBy)), kThreads, 0, st>>>(c, ys,
-                                                                                                 ys + 2 * N);
-        adj_blurT_x_hbar<<<blocks_for(N), kThreads, 0, st>>>(c, ys + 2 * N, img, hbar);
-    } else {
-        cudaError_t e = cudaMemsetAsync(hbar, 0, sizeof(float) * (size_t)N, st);
-        if (e != cudaSuccess) return e;
-    }
-    float *gxb = xs, *gyb = xs + N, *gzb = ys, *nxb = ys + N, *nyb = ys + 2 * N, *nzb = ys + 3 * N;
-    adj_normals<<<blocks_for(N), kThreads, 0, st>>>(c, phi, gxb, gyb, gzb, nxb, nyb, nzb);
-    const dim3 g3((unsigned)((W + kBX - 1) / kBX), (unsigned)((H + kBY - 1) / kBY), (unsigned)L), b3(kBX, kBY, 1);
-    const dim3 gp((unsigned)((W + kBX - 1) / kBX), (unsigned)((H + kBY - 1) / kBY),
-                  (unsigned)((L + kPointZ - 1) / kPointZ));
-    adj_point<<<gp, b3, 0, st>>>(c, phi, img, u, gxb, gyb, gzb, nxb, nyb, nzb, hbar, eo, ei, out, grads);
-    adj_w<<<g3, b3, 0, st>>>(c, phi, u, gxb, gyb, gzb, nxb, nyb, nzb, hbar, eo, ei);
-    adj_gather<<<g3, b3, 0, st>>>(c, hbar, eo, ei, out, flag);
+    c.eps = s.eps;
+    c.dt = s.dt;
+    c.mu = s.mu;
+    c.nu = s.nu;
+    c.l1 = s.l1;
+    c.l2 = s.l2;
+    c.boundary = s.boundary;
+    c.img_f32 = s.img_f32;
+    c.nvol = n;
+    const int n1 = n + 1;
+    auto P = [&](int j) { return pre + (size_t)j * n1; };
+    const dim3 b2(kBX, kBY, 1);
+    if (tot[ADJ_H] > 0) adj_heaviside<<<tot[ADJ_H], kThreads, 0, st>>>(c, vols, P(ADJ_H));
+    if (tot[ADJ_BX] > 0) adj_blur_x<<<tot[ADJ_BX], kThreads, 0, st>>>(c, vols, P(ADJ_BX));
+    if (tot[ADJ_BY] > 0) adj_blur_y<<<tot[ADJ_BY], kThreads, 0, st>>>(c, vols, P(ADJ_BY));
+    if (tot[ADJ_BZ] > 0) adj_blur_z_data<<<tot[ADJ_BZ], kThreads, 0, st>>>(c, vols, P(ADJ_BZ));
+    if (tot[ADJ_TZ] > 0) adj_blurT_z<<<tot[ADJ_TZ], kThreads, 0, st>>>(c, vols, P(ADJ_TZ));
+    if (tot[ADJ_TY] > 0) adj_blurT_y<<<tot[ADJ_TY], kThreads, 0, st>>>(c, vols, P(ADJ_TY));
+    if (tot[ADJ_TX] > 0) adj_blurT_x_hbar<<<tot[ADJ_TX], kThreads, 0, st>>>(c, vols, P(ADJ_TX));
+    if (tot[ADJ_NRM] > 0) adj_normals<<<tot[ADJ_NRM], kThreads, 0, st>>>(c, vols, P(ADJ_NRM));
+    if (tot[ADJ_PT] > 0) adj_point<<<tot[ADJ_PT], b2, 0, st>>>(c, vols, P(ADJ_PT), grads);
+    if (tot[ADJ_W] > 0) adj_w<<<tot[ADJ_W], b2, 0, st>>>(c, vols, P(ADJ_W));
+    if (tot[ADJ_G] > 0) adj_gather<<<tot[ADJ_G], b2, 0, st>>>(c, vols, P(ADJ_G), flag);
     return cudaGetLastError();
 }
 

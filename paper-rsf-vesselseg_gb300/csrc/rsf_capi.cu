@@ -59,6 +59,10 @@ struct rsf_workspace {
     SubVolDev *h_svs = nullptr;  // kStages * max_subvols
     int *h_pre = nullptr;        // kStages * NPRE * (max_subvols + 1)
     unsigned char *h_maps = nullptr;  // kStages * max_subvols * TMAP_BYTES
+    rsf::AdjVol *h_adj = nullptr;     // kStages * max_subvols (adjoint batches)
+    int *h_adj_pre = nullptr;         // kStages * NADJ * (max_subvols + 1)
+    rsf::AdjVol *d_adj = nullptr;
+    int *d_adj_pre = nullptr;
     cudaEvent_t table_ev[kStages] = {};
     bool table_pending[kStages] = {};
     int stage = 0;
@@ -74,6 +78,7 @@ struct rsf_workspace {
         *maps = h_maps + (size_t)stage * max_subvols * rsf::TMAP_BYTES;
         return cudaSuccess;
     }
+    int current_stage() const { return stage; }
     cudaError_t mark_stage(cudaStream_t st) {
         cudaError_t e = cudaEventRecord(table_ev[stage], st);
         if (e == cudaSuccess) {
@@ -190,8 +195,8 @@ rsf_status rsf_gaussian_taps(float sigma, float *taps, int cap, int *k_out) {
 size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols) {
     const size_t v = (size_t)std::max<int64_t>(max_voxels, 0);
     const size_t n = (size_t)std::max<int32_t>(max_subvols, 1);
-    return v * sizeof(float) * 9 + n * (sizeof(SubVolDev) + rsf::TMAP_BYTES) + rsf::NPRE * (n + 1) * sizeof(int) +
-           256;
+    return v * sizeof(float) * 9 + n * (sizeof(SubVolDev) + rsf::TMAP_BYTES + sizeof(rsf::AdjVol)) +
+           (rsf::NPRE + rsf::NADJ) * (n + 1) * sizeof(int) + 256;
 }
 
 static void ws_free(rsf_workspace *ws) {
@@ -208,12 +213,16 @@ static void ws_free(rsf_workspace *ws) {
     cudaFree(ws->d_svs);
     cudaFree(ws->d_pre);
     cudaFree(ws->d_maps);
+    cudaFree(ws->d_adj);
+    cudaFree(ws->d_adj_pre);
     cudaFree(ws->d_flag);
     cudaFree(ws->stage_img);
     cudaFree(ws->stage_phi);
     cudaFreeHost(ws->h_svs);
     cudaFreeHost(ws->h_pre);
     cudaFreeHost(ws->h_maps);
+    cudaFreeHost(ws->h_adj);
+    cudaFreeHost(ws->h_adj_pre);
     for (cudaEvent_t ev : ws->table_ev)
         if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : ws->events) cudaEventDestroy(ev);
@@ -246,12 +255,17 @@ rsf_status rsf_workspace_create(int64_t max_voxels, int32_t max_subvols, rsf_wor
     alloc((void **)&ws->d_svs, (size_t)max_subvols * sizeof(SubVolDev));
     alloc((void **)&ws->d_pre, rsf::NPRE * ((size_t)max_subvols + 1) * sizeof(int));
     alloc((void **)&ws->d_maps, (size_t)max_subvols * rsf::TMAP_BYTES);
+    alloc((void **)&ws->d_adj, (size_t)max_subvols * sizeof(rsf::AdjVol));
+    alloc((void **)&ws->d_adj_pre, rsf::NADJ * ((size_t)max_subvols + 1) * sizeof(int));
     alloc((void **)&ws->d_flag, 256);
     const size_t ns = rsf_workspace::kStages;
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_svs, ns * (size_t)max_subvols * sizeof(SubVolDev));
     if (e == cudaSuccess)
         e = cudaMallocHost((void **)&ws->h_pre, ns * rsf::NPRE * ((size_t)max_subvols + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_maps, ns * (size_t)max_subvols * rsf::TMAP_BYTES);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ws->h_adj, ns * (size_t)max_subvols * sizeof(rsf::AdjVol));
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&ws->h_adj_pre, ns * rsf::NADJ * ((size_t)max_subvols + 1) * sizeof(int));
     for (size_t i = 0; i < ns && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&ws->table_ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws->capture_stream, cudaStreamNonBlocking);
@@ -665,39 +679,147 @@ rsf_status rsf_signed_distance(rsf_workspace *ws, const void *seed, rsf_dtype dt
     return RSF_OK;
 }
 
-// The derivative of one step; kernels and the chain rule are in rsf_adjoint.cu.
-rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
-                            const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
-                            int64_t W, int64_t H, int64_t L, void *stream) {
+// The derivative of one step for a batch; kernels and the chain rule are in
+// rsf_adjoint.cu.
+rsf_status rsf_step_adjoint_batched(rsf_workspace *ws, const rsf_params *p, rsf_dtype dtype,
+                                    const rsf_adjoint_subvol *subvols, int32_t n, double *param_grads,
+                                    void *stream) {
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
+    if (!subvols) return fail(RSF_ERR_INVALID_ARGUMENT, "sub-volume array is null");
+    if (n < 1) return fail(RSF_ERR_INVALID_ARGUMENT, "batch is empty");
+    if (n > ws->max_subvols) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "more sub-volumes than the workspace holds");
     float taps[rsf::MAXK];
     int k = 0;
     rsf_status s = check_params(p, &k, taps);
     if (s != RSF_OK) return s;
-    if ((s = check_shape(W, H, L)) != RSF_OK) return s;
     if ((int)p->sigma2 != 0) return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the box e-term (sigma2 >= 1) is not implemented");
     if (p->data_term != RSF_DATA_TERM_REFERENCE)
         return fail(RSF_ERR_UNSUPPORTED, "the adjoint of the Gaussian data term is not implemented");
-    // the stencil adjoint runs on 3-D grids: one z plane per grid row, 8 y per block
-    if (L > 65535 || H > 65535 * 8) return fail(RSF_ERR_SHAPE, "the adjoint supports L <= 65535 and H <= 524280");
     if (dtype != RSF_U8 && dtype != RSF_F32) return fail(RSF_ERR_DTYPE, "image dtype must be RSF_U8 or RSF_F32");
-    if (!image || !phi || !phi_bar_in || !phi_bar_out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
-    const int64_t n = W * H * L;
-    if (n > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "volume larger than the workspace");
-    auto overlaps = [n](const void *a, size_t abytes, const void *b) {
+    const size_t esz = dtype == RSF_F32 ? 4 : 1;
+    int64_t total = 0;
+    for (int i = 0; i < n; i++) {
+        const rsf_adjoint_subvol &v = subvols[i];
+        if ((s = check_shape(v.W, v.H, v.L)) != RSF_OK) return s;
+        if (!v.image || !v.phi || !v.phi_bar_in || !v.phi_bar_out) return fail(RSF_ERR_INVALID_ARGUMENT, "null pointer");
+        total += v.W * v.H * v.L;
+    }
+    if (total > ws->max_voxels) return fail(RSF_ERR_WORKSPACE_TOO_SMALL, "batch larger than the workspace");
+    // every output must be disjoint from every input and from the other outputs
+    auto overlaps = [](const void *a, size_t abytes, const void *b, size_t bbytes) {
         const char *pa = static_cast<const char *>(a), *pb = static_cast<const char *>(b);
-        return pa < pb + n * sizeof(float) && pb < pa + abytes;
+        return pa < pb + bbytes && pb < pa + abytes;
     };
-    const size_t img_bytes = (size_t)n * (dtype == RSF_F32 ? 4 : 1);
-    if (overlaps(phi_bar_out, n * sizeof(float), phi) || overlaps(phi_bar_out, n * sizeof(float), phi_bar_in) ||
-        overlaps(image, img_bytes, phi_bar_out))
-        return fail(RSF_ERR_INVALID_ARGUMENT, "phi_bar_out overlaps an input");
-    cudaError_t e = rsf::launch_step_adjoint(taps, k, p->eps, p->dt, p->mu, p->nu, p->lambda1, p->lambda2,
-                                             p->boundary, dtype == RSF_F32, phi, image, phi_bar_in, phi_bar_out,
-                                             param_grads, (int)W, (int)H, (int)L, ws->pool_phi2, ws->pool_x,
-                                             ws->pool_y, ws->d_flag, (cudaStream_t)stream);
+    for (int i = 0; i < n; i++) {
+        const rsf_adjoint_subvol &o = subvols[i];
+        const size_t ob = (size_t)(o.W * o.H * o.L) * sizeof(float);
+        for (int j = 0; j < n; j++) {
+            const rsf_adjoint_subvol &v = subvols[j];
+            const size_t nv = (size_t)(v.W * v.H * v.L);
+            if (overlaps(o.phi_bar_out, ob, v.phi, nv * sizeof(float)) ||
+                overlaps(o.phi_bar_out, ob, v.phi_bar_in, nv * sizeof(float)) ||
+                overlaps(o.phi_bar_out, ob, v.image, nv * esz) ||
+                (j != i && overlaps(o.phi_bar_out, ob, v.phi_bar_out, nv * sizeof(float))))
+                return fail(RSF_ERR_INVALID_ARGUMENT, "phi_bar_out overlaps an input or another output");
+        }
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // Specialised tap counts recompute the blurs with the forward step's own
+    // streaming x- and y-passes (pair planes in pool_x, pool_y) and the
+    // z-pass's adjoint variant, which leaves the data-term adjoint pair and
+    // e_out, e_in in each volume's xs slice.
+    const int kspec = rsf::kernel_k(k, RSF_ARITH_PORTABLE, false);
+    // The adjoint's table: volume i's scratch slices at the running voxel
+    // offset (1, 4 and 4 floats per voxel).
+    SubVolDev *h_svs_unused = nullptr;
+    int *h_pre_unused = nullptr;
+    unsigned char *h_maps_unused = nullptr;
+    {
+        cudaError_t e = ws->next_stage(&h_svs_unused, &h_pre_unused, &h_maps_unused);
+        if (e != cudaSuccess) return cuda_fail(e, "table event");
+    }
+    const int stg = ws->current_stage();
+    rsf::AdjVol *h_adj = ws->h_adj + (size_t)stg * ws->max_subvols;
+    int *h_pre = ws->h_adj_pre + (size_t)stg * rsf::NADJ * ((size_t)ws->max_subvols + 1);
+    const int n1 = n + 1;
+    for (int j = 0; j < rsf::NADJ; j++) h_pre[j * n1] = 0;
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        const rsf_adjoint_subvol &v = subvols[i];
+        rsf::AdjVol a;
+        a.phi = v.phi;
+        a.img = v.image;
+        a.u = v.phi_bar_in;
+        a.out = v.phi_bar_out;
+        a.phi2 = ws->pool_phi2 + off;
+        a.xs = ws->pool_x + 4 * off;
+        a.ys = ws->pool_y + 4 * off;
+        a.W = (int)v.W;
+        a.H = (int)v.H;
+        a.L = (int)v.L;
+        int wp = 0;
+        rsf::valid_extents(a.W, a.H, a.L, k, a.Wv, a.Hv, a.Lv, wp);
+        off += (size_t)(v.W * v.H * v.L);
+        int tiles[rsf::NADJ];
+        rsf::adjoint_tiles(a, k, kspec > 0, tiles);
+        for (int j = 0; j < rsf::NADJ; j++) {
+            const int64_t next = (int64_t)h_pre[j * n1 + i] + tiles[j];
+            if (tiles[j] < 0 || next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");
+            h_pre[j * n1 + i + 1] = (int)next;
+        }
+        h_adj[i] = a;
+    }
+    int tot[rsf::NADJ];
+    for (int j = 0; j < rsf::NADJ; j++) tot[j] = h_pre[j * n1 + n];
+    cudaError_t e = cudaMemcpyAsync(ws->d_adj, h_adj, (size_t)n * sizeof(rsf::AdjVol), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ws->d_adj_pre, h_pre, rsf::NADJ * (size_t)n1 * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = ws->mark_stage(st);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint table upload");
+    if (kspec > 0) {
+        std::vector<rsf_subvol> fw((size_t)n);
+        for (int i = 0; i < n; i++)
+            fw[i] = rsf_subvol{const_cast<float *>(subvols[i].phi), subvols[i].image, subvols[i].W, subvols[i].H,
+                               subvols[i].L};
+        int ftot[rsf::NPRE];
+        rsf::LaunchShape sh;
+        const int saved_zt = ws->force_zt;
+        ws->force_zt = 0;  // the adjoint variant streams its planes without TMA
+        s = prepare(ws, fw.data(), n, k, kspec, 0, 0, dtype, nullptr, ftot, &sh, st);
+        ws->force_zt = saved_zt;
+        if (s != RSF_OK) return s;
+        const StepConst c = make_const(p, k, taps, dtype, n, sh, nullptr);
+        const SubVolDev *svs = ws->d_svs;
+        const int *pre = ws->d_pre;
+        const int f1 = n + 1;
+        if (ftot[0] > 0) switch (kspec) {
+                case 21: e = rsf::launch_xpass_21(svs, pre, ftot[0], c, 0, RSF_ARITH_PORTABLE, st); break;
+                case 29: e = rsf::launch_xpass_29(svs, pre, ftot[0], c, 0, RSF_ARITH_PORTABLE, st); break;
+                default: e = rsf::launch_xpass_35(svs, pre, ftot[0], c, 0, RSF_ARITH_PORTABLE, st); break;
+            }
+        if (e == cudaSuccess && ftot[1] > 0) switch (kspec) {
+                case 21: e = rsf::launch_ypass_21(svs, pre + f1, ftot[1], c, st); break;
+                case 29: e = rsf::launch_ypass_29(svs, pre + f1, ftot[1], c, st); break;
+                default: e = rsf::launch_ypass_35(svs, pre + f1, ftot[1], c, st); break;
+            }
+        if (e == cudaSuccess && ftot[2] > 0) switch (kspec) {
+                case 21: e = rsf::launch_zpass_adjoint_21(svs, pre + 2 * f1, ftot[2], c, ws->d_adj, st); break;
+                case 29: e = rsf::launch_zpass_adjoint_29(svs, pre + 2 * f1, ftot[2], c, ws->d_adj, st); break;
+                default: e = rsf::launch_zpass_adjoint_35(svs, pre + 2 * f1, ftot[2], c, ws->d_adj, st); break;
+            }
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint blur recompute launch");
+    }
+    const rsf::AdjScalars sc = {p->eps, p->dt, p->mu, p->nu, p->lambda1, p->lambda2, p->boundary, dtype == RSF_F32};
+    e = rsf::launch_step_adjoint(taps, k, sc, ws->d_adj, ws->d_adj_pre, n, tot, param_grads, ws->d_flag, st);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
     return RSF_OK;
+}
+
+rsf_status rsf_step_adjoint(rsf_workspace *ws, const rsf_params *p, const void *image, rsf_dtype dtype,
+                            const float *phi, const float *phi_bar_in, float *phi_bar_out, double *param_grads,
+                            int64_t W, int64_t H, int64_t L, void *stream) {
+    const rsf_adjoint_subvol v = {phi, image, phi_bar_in, phi_bar_out, W, H, L};
+    return rsf_step_adjoint_batched(ws, p, dtype, &v, 1, param_grads, stream);
 }
 
 // Grid checks on the host; the gather itself is in rsf_reassemble.cu.  The

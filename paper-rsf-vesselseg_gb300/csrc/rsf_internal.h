@@ -140,6 +140,26 @@ int sm_count();
 void set_last_error(const char *msg);
 
 // Per-kernel launchers; each tap specialisation lives in its own object file.
+// One volume of an adjoint batch (rsf_adjoint.cu), N = W H L.
+struct AdjVol {
+    const float *phi;  // the step's input level set
+    const void *img;
+    const float *u;    // dL/dphi' of the step's output
+    float *out;        // dL/dphi
+    float *phi2;       // scratch, N floats
+    float *xs, *ys;    // scratch, 4 N floats each
+    int W, H, L;
+    int Wv, Hv, Lv;    // valid blur extents; all > 0 or all 0
+};
+// Adjoint kernels with a block prefix array each (rsf_adjoint.cu): H, the
+// recompute blurs x, y, z, the transposed blurs z, y, x, normals, pointwise
+// terms, w, gather.
+constexpr int NADJ = 11;
+enum AdjKernel { ADJ_H, ADJ_BX, ADJ_BY, ADJ_BZ, ADJ_TZ, ADJ_TY, ADJ_TX, ADJ_NRM, ADJ_PT, ADJ_W, ADJ_G };
+// Blocks of each adjoint kernel for one volume; with `streamed` the
+// recompute (ADJ_H .. ADJ_BZ) runs in the forward step's kernels instead.
+void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]);
+
 #define RSF_DECLARE_K(K)                                                                                      \
     cudaError_t launch_xpass_##K(const SubVolDev *, const int *, int, const StepConst &, int, int, cudaStream_t); \
     cudaError_t config_xpass_##K();                                                                             \
@@ -151,6 +171,14 @@ RSF_DECLARE_K(21)
 RSF_DECLARE_K(29)
 RSF_DECLARE_K(35)
 #undef RSF_DECLARE_K
+// The streaming z-pass with the adjoint's emit (pair planes, specialised k):
+// sub-volume i of the table is volume i of `vols`.
+cudaError_t launch_zpass_adjoint_21(const SubVolDev *, const int *, int, const StepConst &, const AdjVol *vols,
+                                    cudaStream_t);
+cudaError_t launch_zpass_adjoint_29(const SubVolDev *, const int *, int, const StepConst &, const AdjVol *vols,
+                                    cudaStream_t);
+cudaError_t launch_zpass_adjoint_35(const SubVolDev *, const int *, int, const StepConst &, const AdjVol *vols,
+                                    cudaStream_t);
 cudaError_t config_ztpass_21();
 cudaError_t config_ztpass_35();
 cudaError_t launch_ztpass_21(const SubVolDev *, const int *, int, const StepConst &, unsigned *flag, cudaStream_t);
@@ -163,12 +191,16 @@ cudaError_t launch_gauss(const SubVolDev *, const int *pre, int n1, const int *t
                          const DebugOut *dbg, cudaStream_t);
 // Box e-term (c.box >= 1): data factor of every voxel, stencil tiling.
 cudaError_t launch_box(const SubVolDev *, const int *, int, const StepConst &, const DebugOut *dbg, cudaStream_t);
-// Reverse-mode derivative of one step (rsf_adjoint.cu); scratch from the
-// workspace pools phi2 (N floats), xs (4N) and ys (4N).
-cudaError_t launch_step_adjoint(const float *taps, int k, float eps, float dt, float mu, float nu, float l1, float l2,
-                                int boundary, int img_f32, const float *phi, const void *img, const float *u,
-                                float *out, double *grads, int W, int H, int L, float *phi2, float *xs, float *ys,
-                                unsigned *flag, cudaStream_t st);
+// Reverse-mode derivative of one step for a batch of volumes (rsf_adjoint.cu).
+// vols: n entries (device); pre: NADJ block prefix arrays of n + 1 entries
+// (device); tot: their totals.  Parameter sums over the batch are added to
+// grads[0..3] when grads is not null.
+struct AdjScalars {
+    float eps, dt, mu, nu, l1, l2;
+    int boundary, img_f32;
+};
+cudaError_t launch_step_adjoint(const float *taps, int k, const AdjScalars &s, const AdjVol *vols, const int *pre,
+                                int n, const int *tot, double *grads, unsigned *flag, cudaStream_t st);
 // Reassembly (rsf_reassemble.cu): one evolved sub-volume placed in the output.
 constexpr int RA_MAXCELLS = 64;  // grid cells per axis
 struct TileDev {

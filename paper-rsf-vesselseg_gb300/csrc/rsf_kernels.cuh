@@ -533,14 +533,13 @@ __device__ __forceinline__ void fits_and_data(const SubVolDev &s, const StepCons
     }
 }
 
-template <int K, bool DEBUG, bool PAIRS = false>
-__global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__restrict__ svs,
-                                                             const int *__restrict__ pre, const StepConst c,
-                                                             DebugOut dbg) {
-    const int b = blockIdx.x;
-    const int sv = find_sv(pre, c.nsv, b);
-    const SubVolDev s = svs[sv];
-    int t = b - __ldg(pre + sv);
+// The streaming z-pass of one block (tile t of sub-volume s): every lane
+// gets its column's blurred pair at each output plane o and the image there,
+// and hands them to fits(f, x, y, o, live, I, B), which all lanes of the warp
+// call together (it may shuffle), for o = 0, 1, ..., Lv - 1 in order.
+// begin(xc, y, live) runs first, with the lane's output column xc.
+template <int K, bool PAIRS, class Begin, class Fits>
+__device__ __forceinline__ void zpass_body(const SubVolDev &s, const StepConst &c, int t, Begin begin, Fits fits) {
     const int ntx = (s.Wv + 2 * ZP_PAIRS - 1) / (2 * ZP_PAIRS);
     const int tx = t % ntx;
     const int y = t / ntx;
@@ -563,6 +562,7 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
     const unsigned char *img0 = static_cast<const unsigned char *>(s.img) +
                                 (((size_t)(y + c.r)) * s.W + (size_t)(xc + c.r)) * esz;
     const size_t sstride = (size_t)s.W * s.H * esz;
+    begin(xc, y, live);
     if constexpr (K % ring_depth(K) == 0 && ring_depth(K) != RING) {
         constexpr int RD = ring_depth(K);
         RingC<RD> rg = {ring + threadIdx.x, ZP_PAIRS * 4, src, pstride, 0, s.L, act};
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
                 if (c.img_f32) I = __uint_as_float(wd);
                 else I = (float)((wd >> (8 * ((shift0 + (unsigned)o * shift_step) & 3u))) & 0xffu);
             }
-            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+            fits(f, x, y, o, live, I, v);
         };
         stream_axis_c<K, RD>(rg, c, emit);
     } else {
@@ -600,10 +600,119 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
                 if (c.img_f32) I = __uint_as_float(wd);
                 else I = (float)((wd >> (8 * (unsigned)(reinterpret_cast<uintptr_t>(rg.sbyte(i)) & 3))) & 0xffu);
             }
-            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+            fits(f, x, y, o, live, I, v);
         };
         stream_axis<K>(rg, c, emit);
     }
+}
+
+template <int K, bool DEBUG, bool PAIRS = false>
+__global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__restrict__ svs,
+                                                             const int *__restrict__ pre, const StepConst c,
+                                                             DebugOut dbg) {
+    const int b = blockIdx.x;
+    const int sv = find_sv(pre, c.nsv, b);
+    const SubVolDev s = svs[sv];
+    zpass_body<K, PAIRS>(
+        s, c, b - __ldg(pre + sv), [](int, int, bool) {},
+        [&](int f, int x, int y, int o, bool live, float I, float2 v) {
+            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, dbg, DEBUG);
+        });
+}
+
+// The adjoint's recompute of the fits (rsf_adjoint.cu): the forward z-pass
+// over pair planes, emitting at each valid voxel, instead of the data factor,
+//   e_out = (I - f_out)^2 and e_in at the full-volume index, and the pair
+//   (B1_bar - B3_bar, B2_bar - B4_bar) in the valid layout (row stride Wv),
+// with B1..B4 the blurs of I H, H, I (1-H), 1-H, f_out = B1 / B2,
+// f_in = B3 / B4, and for data_bar = -u dt delta(phi)
+//   f_out_bar = -2 (I - f_out) lambda1 data_bar, f_in_bar = 2 (I - f_in) lambda2 data_bar,
+//   B1_bar = f_out_bar / B2, B2_bar = -f_out_bar f_out / B2 (B3, B4 alike).
+// ph, uo: phi and u at the lane's voxel of output plane o.  The pair goes to
+// a.xs (2 Wv Hv Lv floats), e_out and e_in to a.xs + 2 N and a.xs + 3 N.
+__device__ __forceinline__ void adjoint_fits(const SubVolDev &s, const StepConst &c, const AdjVol &a, int f, int x,
+                                             int y, int o, bool live, float I, float2 B, float ph, float uo) {
+    // lanes as in fits_and_data's pair layout: 0, 1 -> f_out at x, x + 1;
+    // 2, 3 -> f_in at x, x + 1
+    const float bx_hi = __shfl_down_sync(0xffffffffu, B.x, 2);
+    const float by_lo = __shfl_up_sync(0xffffffffu, B.y, 2);
+    const bool outer = f < 2;
+    const float num = outer ? bx_hi : B.y;
+    const float den = outer ? B.x : by_lo;
+    const int xc = x + (f & 1);
+    const size_t vi = ((size_t)(o + c.r) * s.H + (y + c.r)) * s.W + (xc + c.r);
+    float bn = 0.0f, bd = 0.0f, e = 0.0f;
+    if (live) {
+        const float rb = __frcp_rn(den);
+        const float fv = num * rb;
+        const float d = I - fv;
+        e = d * d;
+        const float delta = __fdividef(0.318309886183790672f * c.eps, fmaf(ph, ph, c.eps * c.eps));
+        const float data_bar = -uo * c.dt * delta;
+        const float fbar = -2.0f * d * (outer ? c.l1 * data_bar : -c.l2 * data_bar);
+        bn = fbar * rb;
+        bd = -fbar * fv * rb;
+    }
+    const float bn_in = __shfl_down_sync(0xffffffffu, bn, 2);
+    const float bd_in = __shfl_down_sync(0xffffffffu, bd, 2);
+    if (live) {
+        const size_t n = (size_t)s.W * s.H * s.L;
+        if (outer) {
+            const size_t nv = (size_t)s.Wv * s.Hv * s.Lv;
+            const size_t vo = ((size_t)o * s.Hv + y) * s.Wv + xc;
+            a.xs[vo] = bn - bn_in;
+            a.xs[nv + vo] = bd - bd_in;
+            a.xs[2 * n + vi] = e;
+        } else {
+            a.xs[3 * n + vi] = e;
+        }
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_adjoint_kernel(const SubVolDev *__restrict__ svs,
+                                                                     const int *__restrict__ pre, const StepConst c,
+                                                                     const AdjVol *__restrict__ vols) {
+    const int b = blockIdx.x;
+    const int sv = find_sv(pre, c.nsv, b);
+    const SubVolDev s = svs[sv];
+    const AdjVol a = vols[sv];
+    // phi and u of output planes o, o + 1, o + 2 ride in registers: each
+    // output's loads are issued three planes ahead (the streaming loop is
+    // latency-bound when the volume gives few blocks per SM).
+    const size_t plane = (size_t)s.W * s.H;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, u0 = 0.f, u1 = 0.f, u2 = 0.f;
+    size_t vnext = 0;  // offset of the lane's voxel in plane o + 3 + r
+    auto begin = [&](int xc, int y, bool live) {
+        const size_t v0 = ((size_t)c.r * s.H + (y + c.r)) * s.W + (xc + c.r);
+        if (live) {
+            p0 = __ldg(a.phi + v0);
+            u0 = __ldg(a.u + v0);
+            if (s.Lv > 1) {
+                p1 = __ldg(a.phi + v0 + plane);
+                u1 = __ldg(a.u + v0 + plane);
+            }
+            if (s.Lv > 2) {
+                p2 = __ldg(a.phi + v0 + 2 * plane);
+                u2 = __ldg(a.u + v0 + 2 * plane);
+            }
+        }
+        vnext = v0 + 3 * plane;
+    };
+    zpass_body<K, true>(s, c, b - __ldg(pre + sv), begin,
+                        [&](int f, int x, int y, int o, bool live, float I, float2 v) {
+                            const float ph = p0, uo = u0;
+                            p0 = p1;
+                            u0 = u1;
+                            p1 = p2;
+                            u1 = u2;
+                            if (live && o + 3 < s.Lv) {
+                                p2 = __ldg(a.phi + vnext);
+                                u2 = __ldg(a.u + vnext);
+                            }
+                            vnext += plane;
+                            adjoint_fits(s, c, a, f, x, y, o, live, I, v, ph, uo);
+                        });
 }
 
 template <bool DEBUG>

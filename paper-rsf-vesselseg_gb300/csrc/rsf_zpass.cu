@@ -1,6 +1,8 @@
 // rsf_zpass.cu -- z-pass (local fits and data factor) for one tap count
 // (compiled once per -DRSF_K value; RSF_K = 0 is the run-time-k kernel, which
-// also writes the debug fields).
+// also writes the debug fields).  The specialised tap counts also carry the
+// adjoint's variant, which emits the data-term adjoint instead of the data
+// factor.
 #include "rsf_kernels.cuh"
 
 #ifndef RSF_K
@@ -24,5 +26,13 @@ cudaError_t RSF_CAT(launch_zpass_, RSF_K)(const SubVolDev *svs, const int *pre, 
 #endif
     return cudaGetLastError();
 }
+
+#if RSF_K > 0
+cudaError_t RSF_CAT(launch_zpass_adjoint_, RSF_K)(const SubVolDev *svs, const int *pre, int blocks,
+                                                  const StepConst &c, const AdjVol *vols, cudaStream_t st) {
+    zpass_adjoint_kernel<RSF_K><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, vols);
+    return cudaGetLastError();
+}
+#endif
 
 }  // namespace rsf

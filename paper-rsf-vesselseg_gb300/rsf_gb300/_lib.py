@@ -32,6 +32,11 @@ class RsfSubvol(ctypes.Structure):
                 ("H", ctypes.c_int64), ("L", ctypes.c_int64)]
 
 
+class RsfAdjointSubvol(ctypes.Structure):
+    _fields_ = [("phi", ctypes.c_void_p), ("image", ctypes.c_void_p), ("phi_bar_in", ctypes.c_void_p),
+                ("phi_bar_out", ctypes.c_void_p), ("W", ctypes.c_int64), ("H", ctypes.c_int64), ("L", ctypes.c_int64)]
+
+
 class RsfTile(ctypes.Structure):
     _fields_ = [("phi", ctypes.c_void_p), ("x0", ctypes.c_int64), ("y0", ctypes.c_int64), ("z0", ctypes.c_int64),
                 ("W", ctypes.c_int64), ("H", ctypes.c_int64), ("L", ctypes.c_int64)]
@@ -71,6 +76,8 @@ SIGNATURES = {
     "rsf_copy_async": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "rsf_step_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), _P, ctypes.c_int, _P, _P, _P, _P, _I64, _I64,
                                         _I64, _P]),
+    "rsf_step_adjoint_batched": (ctypes.c_int, [_P, ctypes.POINTER(RsfParams), ctypes.c_int,
+                                                ctypes.POINTER(RsfAdjointSubvol), _I32, _P, _P]),
     "rsf_set_kernel_timing": (ctypes.c_int, [_P, ctypes.c_int]),
     "rsf_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                         ctypes.c_int]),

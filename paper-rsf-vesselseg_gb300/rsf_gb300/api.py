@@ -15,7 +15,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import RsfParams, RsfSubvol, check
+from ._lib import RsfAdjointSubvol, RsfParams, RsfSubvol, check
 
 
 @dataclass
@@ -181,6 +181,39 @@ class Workspace:
                                          ctypes.c_void_p(phi_bar.data_ptr()), ctypes.c_void_p(out.data_ptr()), gp,
                                          W, H, L, ctypes.c_void_p(_stream_ptr(stream))))
         return out
+
+    def step_adjoint_batched(self, items, params: Params, param_grads=None, stream=None):
+        """`step_adjoint` for a list of (image, phi, phi_bar, out) CUDA tensor
+        tuples in one launch sequence; `out` (may be None) receives dL/dphi of
+        its volume.  Parameter gradients, summed over the batch, are added to
+        `param_grads` when given.  Returns the list of outputs."""
+        import torch
+        if not items:
+            raise ValueError("empty batch")
+        codes = {_dtype_code(img.dtype) for img, _, _, _ in items}
+        if len(codes) != 1:
+            raise TypeError("all images of a batch must share one dtype")
+        arr = (RsfAdjointSubvol * len(items))()
+        outs = []
+        for i, (img, phi, pbar, out) in enumerate(items):
+            _require_cuda(img, phi, pbar)
+            _require_volume(phi, img, pbar)
+            if out is None:
+                out = torch.empty_like(phi)
+            _require_cuda(out)
+            _require_volume(out, phi)
+            L, H, W = phi.shape
+            arr[i] = RsfAdjointSubvol(phi.data_ptr(), img.data_ptr(), pbar.data_ptr(), out.data_ptr(), W, H, L)
+            outs.append(out)
+        gp = None
+        if param_grads is not None:
+            _require_cuda(param_grads)
+            if param_grads.dtype != torch.float64 or param_grads.numel() < 4:
+                raise TypeError("param_grads must be a CUDA float64 tensor of 4 elements")
+            gp = ctypes.c_void_p(param_grads.data_ptr())
+        check(self._lib.rsf_step_adjoint_batched(self.handle, ctypes.byref(params.to_c()), codes.pop(), arr,
+                                                 len(items), gp, ctypes.c_void_p(_stream_ptr(stream))))
+        return outs
 
     def evolve_batched(self, pairs, params: Params, iters: int, stream=None):
         """Evolves a list of (image, phi) CUDA tensor pairs, each phi in place."""

@@ -4,6 +4,10 @@
 `Workspace.evolve` and returns phi_T as a tensor that autograd can
 differentiate with respect to phi0 and to lambda1, lambda2, mu, nu.
 
+A batch of volumes of one shape, phi0 and image of shape (B, L, H, W), runs
+as one batch: `rsf_evolve_batched` forward and `rsf_step_adjoint_batched`
+backward, one launch sequence per step for the whole batch.
+
 Forward keeps phi every `checkpoint_every` steps (T / C + 1 volumes).
 Backward walks the segments from the last: it recomputes the segment's
 states from its checkpoint with the forward kernels (bit-identical to the
@@ -20,6 +24,14 @@ import torch
 from .api import Params, Workspace
 
 _PARAM_NAMES = ("lambda1", "lambda2", "mu", "nu")
+
+
+def _step(ws: Workspace, image: torch.Tensor, phi: torch.Tensor, p: Params, n: int) -> None:
+    """n iterations of phi in place: one volume (L, H, W) or a batch (B, L, H, W)."""
+    if image.dim() == 4:
+        ws.evolve_batched(list(zip(image.unbind(0), phi.unbind(0))), p, n)
+    else:
+        ws.evolve(image, phi, p, n)
 
 
 class _Evolve(torch.autograd.Function):
@@ -40,7 +52,7 @@ class _Evolve(torch.autograd.Function):
         while t < iters:
             ckpts.append(phi.clone())
             n = min(every, iters - t)
-            ws.evolve(image, phi, p, n)
+            _step(ws, image, phi, p, n)
             t += n
         ctx.save_for_backward(image, *ckpts)
         ctx.p, ctx.iters, ctx.every, ctx.ws = p, iters, every, ws
@@ -59,10 +71,14 @@ class _Evolve(torch.autograd.Function):
             states = [ckpts[s]]
             for _ in range(1, n):
                 nxt = states[-1].clone()
-                ws.evolve(image, nxt, p, 1)
+                _step(ws, image, nxt, p, 1)
                 states.append(nxt)
             for i in reversed(range(n)):
-                ws.step_adjoint(image, states[i], u, p, out=tmp, param_grads=g)
+                if image.dim() == 4:
+                    ws.step_adjoint_batched(list(zip(image.unbind(0), states[i].unbind(0), u.unbind(0),
+                                                     tmp.unbind(0))), p, param_grads=g)
+                else:
+                    ws.step_adjoint(image, states[i], u, p, out=tmp, param_grads=g)
                 u, tmp = tmp, u
         out = [u if ctx.needs_input_grad[0] else None, None]
         for k, (dtype, device, shape) in enumerate(ctx.pmeta):
@@ -74,14 +90,17 @@ def evolve(phi0: torch.Tensor, image: torch.Tensor, params: Params, iters: int, 
            nu=None, checkpoint_every: int = 10, workspace: Workspace | None = None) -> torch.Tensor:
     """phi_T after `iters` steps, differentiable in phi0 and in any of
     lambda1, lambda2, mu, nu passed as tensors (others come from `params`).
-    phi0 and image are CUDA tensors (L, H, W); image uint8 or float32.
+    phi0 and image are CUDA tensors (L, H, W), or (B, L, H, W) for a batch
+    that shares the parameters; image uint8 or float32.
     Parameter tensors on the host are read without synchronising the device;
     CUDA parameter tensors cost one device-to-host transfer per call."""
     if iters < 1:
         raise ValueError("iters must be >= 1")
     if checkpoint_every < 1:
         raise ValueError("checkpoint_every must be >= 1")
-    ws = workspace if workspace is not None else Workspace(phi0.numel())
+    if phi0.dim() not in (3, 4) or image.shape != phi0.shape:
+        raise ValueError("phi0 and image must both be (L, H, W) or both (B, L, H, W)")
+    ws = workspace if workspace is not None else Workspace(phi0.numel(), phi0.shape[0] if phi0.dim() == 4 else 1)
     args = []
     for name, v in zip(_PARAM_NAMES, (lambda1, lambda2, mu, nu)):
         # parameters that are not tensors become host scalars (no gradient)
