@@ -106,7 +106,7 @@ __device__ __forceinline__ NormDen norm_den(float mag) {
         const float bb = __fsub_rn(d.s, mag);
         const float err = __fadd_rn(__fsub_rn(mag, __fsub_rn(d.s, bb)), __fsub_rn(EPS6_HI, bb));
         d.dlo = __fadd_rn(err, EPS6_LO);
-        d.rinv = __fdiv_rn(1.0f, d.s);
+        d.rinv = __frcp_rn(d.s);  // the correctly rounded 1 / s, as 1.0f / s
         d.dref = 0.0;
     }
     return d;

@@ -878,7 +878,7 @@ __device__ __forceinline__ float st_data(const StencilCtx &k, const StepConst &c
 
 template <int C, Arith A, bool DEBUG>
 __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepConst &c, StencilState &S, int rel,
-                                             float (*Pb)[ST_WARPS][32], float (*Gb)[2][ST_WARPS][32],
+                                             float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
                                              unsigned *flag, const DebugOut &dbg) {
     constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
     const int sc = k.first + rel;  // output plane of this step
@@ -904,8 +904,7 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
         gn = gn_from<A>(xl, xr, yl, yr, zl, zr);
     }
     S.G[C1] = GN4{gn.nx, gn.gx, gn.nz, gn.gz};
-    Gb[C1][0][k.w][k.lane] = gn.ny;
-    Gb[C1][1][k.w][k.lane] = gn.gy;
+    Gb[C1][k.w][k.lane] = make_float2(gn.ny, gn.gy);
     __syncthreads();
     const GN4 &gc = S.G[C];
     const float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
@@ -927,8 +926,8 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
         const bool xr_in = k.x < k.W - 1;
         const float nxr = xr_in ? nxR : gc.nx, gxr = xr_in ? gxR : gc.gx;
         const int wl = k.y > 0 ? k.w - 1 : k.w, wr = k.y < k.H - 1 ? k.w + 1 : k.w;
-        const float nyl = Gb[C][0][wl][k.lane], nyr = Gb[C][0][wr][k.lane];
-        const float gyl = Gb[C][1][wl][k.lane], gyr = Gb[C][1][wr][k.lane];
+        const float2 yl2 = Gb[C][wl][k.lane], yr2 = Gb[C][wr][k.lane];
+        const float nyl = yl2.x, nyr = yr2.x, gyl = yl2.y, gyr = yr2.y;
         const GN4 &gp = S.G[C2];
         const float nzl = sc > 0 ? gp.nz : gc.nz, nzr = sc < k.L - 1 ? gn.nz : gc.nz;
         const float gzl = sc > 0 ? gp.gz : gc.gz, gzr = sc < k.L - 1 ? gn.gz : gc.gz;
@@ -954,7 +953,7 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
             dbg.f[4 * dbg.n + vi] = dh;
             dbg.f[5 * dbg.n + vi] = kap;
             dbg.f[6 * dbg.n + vi] = lap;
-            dbg.f[7 * dbg.n + vi] = grad_mag(gc.gx, Gb[C][1][k.w][k.lane], gc.gz);
+            dbg.f[7 * dbg.n + vi] = grad_mag(gc.gx, Gb[C][k.w][k.lane].y, gc.gz);
         }
     }
     S.P[C] = p3;    // plane rel+3
@@ -969,18 +968,31 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
 // inside).  The per-thread boundary selects and bounds tests drop out; the z
 // rules depend only on the plane, so they stay as block-uniform tests; phi is
 // read and written through pointers that advance one plane per step.
-template <int C, Arith A>
+// INSIDE: the block's outputs all lie in the valid region (blk_inside), and
+// dp walks the thread's column of the data factor one plane per step.
+// EDGE: the step may meet a z rule or an end of the block's plane range
+// (steps of the first and last groups of three, and groups near the first or
+// last plane of the volume); otherwise every plane test is known to pass.
+// acc collects out * 0, which is NaN once any output is not finite.
+template <int C, Arith A, bool INSIDE, bool EDGE>
 __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepConst &c, StencilState &S, int sc,
-                                                const float *&pp, float *&op, float (*Pb)[ST_WARPS][32],
-                                                float (*Gb)[2][ST_WARPS][32], unsigned *flag) {
+                                                const float *&pp, float *&op, const float *&dp,
+                                                float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
+                                                float &acc) {
     constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
     float p3 = 0.0f, exn = 0.0f, eyn = 0.0f;  // plane sc + 3
-    if (sc + 3 < k.L) {
+    if (!EDGE || sc + 3 < k.L) {
         p3 = __ldg(pp);
         if (k.need_x) exn = __ldg(pp + k.xoff);
         if (k.need_y) eyn = __ldg(pp + k.yoff);
     }
-    const float dn = st_data(k, c, sc + 1);
+    float dn;  // data factor of plane sc + 1
+    if constexpr (INSIDE) {
+        dn = (k.outp && (!EDGE || (sc + 1 >= k.z0 && sc + 1 < k.z1))) ? __ldg(dp) : 0.0f;
+        dp += k.dplane;
+    } else {
+        dn = st_data(k, c, sc + 1);
+    }
     pp += k.WH;
     Pb[C2][k.w][k.lane] = S.P[C2];
     const float p0 = S.P[C], p1 = S.P[C1], p2 = S.P[C2];
@@ -993,19 +1005,18 @@ __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepC
     // gradient of plane pn = sc + 1 (z rules at the first and last plane; a
     // plane outside the volume gets a value that no output reads)
     const int pn = sc + 1;
-    const GN gn = gn_from<A>(L1, R1, U1, D1, pn > 0 ? p0 : p1, pn < k.L - 1 ? p2 : p1);
+    const GN gn = gn_from<A>(L1, R1, U1, D1, (!EDGE || pn > 0) ? p0 : p1, (!EDGE || pn < k.L - 1) ? p2 : p1);
     S.G[C1] = GN4{gn.nx, gn.gx, gn.nz, gn.gz};
-    Gb[C1][0][k.w][k.lane] = gn.ny;
-    Gb[C1][1][k.w][k.lane] = gn.gy;
+    Gb[C1][k.w][k.lane] = make_float2(gn.ny, gn.gy);
     __syncthreads();
     const GN4 &gc = S.G[C];
     const float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
     const float gxL = __shfl_up_sync(0xffffffffu, gc.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gc.gx, 1);
-    if (sc >= k.z0 && k.outp) {
-        const float nyl = Gb[C][0][k.w - 1][k.lane], nyr = Gb[C][0][k.w + 1][k.lane];
-        const float gyl = Gb[C][1][k.w - 1][k.lane], gyr = Gb[C][1][k.w + 1][k.lane];
+    if ((!EDGE || sc >= k.z0) && k.outp) {
+        const float2 yl2 = Gb[C][k.w - 1][k.lane], yr2 = Gb[C][k.w + 1][k.lane];
+        const float nyl = yl2.x, nyr = yr2.x, gyl = yl2.y, gyr = yr2.y;
         const GN4 &gp = S.G[C2];
-        const bool zlo = sc > 0, zhi = sc < k.L - 1;
+        const bool zlo = !EDGE || sc > 0, zhi = !EDGE || sc < k.L - 1;
         const float nzl = zlo ? gp.nz : gc.nz, nzr = zhi ? gn.nz : gc.nz;
         const float gzl = zlo ? gp.gz : gc.gz, gzr = zhi ? gn.gz : gc.gz;
         const float kap = __fadd_rn(__fadd_rn(half_diff(nxR, nxL), half_diff(nyr, nyl)), half_diff(nzr, nzl));
@@ -1013,13 +1024,36 @@ __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepC
         const float dh = dirac<A>(p0, c.eps);
         const float out = update_phi(p0, dh, S.DT[C], kap, lap, c.dt, c.nu, c.mu);
         *op = out;
-        if (!isfinite(out)) atomicOr(flag, kFlagNonFinite);
+        acc = __fmaf_rn(out, 0.0f, acc);
     }
     op += k.WH;
     S.P[C] = p3;
     S.EX[C] = exn;
     S.EY[C] = eyn;
     S.DT[C1] = dn;
+}
+
+// The steps of an x/y-interior block in groups of three (one per ring
+// slot); groups that can meet no z rule and no end of the plane range run
+// without the plane tests.
+template <Arith A, bool INSIDE>
+__device__ __forceinline__ void stencil_planes_in(const StencilCtx &k, const StepConst &c, StencilState &S, int count,
+                                                  const float *&pp, float *&op, const float *&dp,
+                                                  float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
+                                                  float &acc) {
+    for (int i = 0; i < count; i += 3) {
+        const int sc = k.first + i;
+        const bool edge = i == 0 || i + 3 >= count || sc <= 0 || sc + 5 >= k.L;
+        if (edge) {
+            stencil_step_in<0, A, INSIDE, true>(k, c, S, sc, pp, op, dp, Pb, Gb, acc);
+            if (i + 1 < count) stencil_step_in<1, A, INSIDE, true>(k, c, S, sc + 1, pp, op, dp, Pb, Gb, acc);
+            if (i + 2 < count) stencil_step_in<2, A, INSIDE, true>(k, c, S, sc + 2, pp, op, dp, Pb, Gb, acc);
+        } else {
+            stencil_step_in<0, A, INSIDE, false>(k, c, S, sc, pp, op, dp, Pb, Gb, acc);
+            stencil_step_in<1, A, INSIDE, false>(k, c, S, sc + 1, pp, op, dp, Pb, Gb, acc);
+            stencil_step_in<2, A, INSIDE, false>(k, c, S, sc + 2, pp, op, dp, Pb, Gb, acc);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1092,7 +1126,7 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
                                                                    const StepConst c, int parity,
                                                                    unsigned *__restrict__ flag, DebugOut dbg) {
     __shared__ float Pb[3][ST_WARPS][32];
-    __shared__ float Gb[3][2][ST_WARPS][32];
+    __shared__ float2 Gb[3][ST_WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;
     const int sv = find_sv(pre, c.nsv, b);
@@ -1169,11 +1203,12 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     if (interior) {
         const float *pp = k.phi + (ptrdiff_t)(k.first + 3) * (ptrdiff_t)k.WH;
         float *op = k.phi_out + (ptrdiff_t)k.first * (ptrdiff_t)k.WH + (ptrdiff_t)k.col;
-        for (int i = 0; i < count; i += 3) {
-            stencil_step_in<0, A>(k, c, S, k.first + i, pp, op, Pb, Gb, flag);
-            if (i + 1 < count) stencil_step_in<1, A>(k, c, S, k.first + i + 1, pp, op, Pb, Gb, flag);
-            if (i + 2 < count) stencil_step_in<2, A>(k, c, S, k.first + i + 2, pp, op, Pb, Gb, flag);
-        }
+        // plane first + 1 of the data column (read only from plane z0 on)
+        const float *dp = k.dcol + ((ptrdiff_t)k.first + 1 - k.r) * (ptrdiff_t)k.dplane;
+        float acc = 0.0f;
+        if (k.blk_inside) stencil_planes_in<A, true>(k, c, S, count, pp, op, dp, Pb, Gb, acc);
+        else stencil_planes_in<A, false>(k, c, S, count, pp, op, dp, Pb, Gb, acc);
+        if (!isfinite(acc)) atomicOr(flag, kFlagNonFinite);
         return;
     }
     for (int i = 0; i < count; i += 3) {
