@@ -837,6 +837,11 @@ struct StencilCtx {
     bool need_x, need_y;
     ptrdiff_t xoff, yoff;   // offsets of the extra neighbour loads
     size_t col;
+    // fast path (stencil_step_f): rows of the y neighbours in the shared
+    // rings, and the x face rules of the thread's voxel
+    int urow, drow;         // phi rows above / below (Pb, ST_WARPS + 2 rows)
+    int gwl, gwr;           // gradient rows above / below (Gb)
+    bool xl_self, xr_self;  // the x - 1 / x + 1 neighbour is the voxel itself
 };
 
 // nx, gx, nz, gz of a plane (ny, gy live in the shared rows)
@@ -878,7 +883,7 @@ __device__ __forceinline__ float st_data(const StencilCtx &k, const StepConst &c
 
 template <int C, Arith A, bool DEBUG>
 __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepConst &c, StencilState &S, int rel,
-                                             float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
+                                             float (*Pb)[ST_WARPS + 2][32], float2 (*Gb)[ST_WARPS][32],
                                              unsigned *flag, const DebugOut &dbg) {
     constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
     const int sc = k.first + rel;  // output plane of this step
@@ -887,14 +892,14 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
     const float p3 = st_ld(k, sc + 3);
     const float exn = st_ldx(k, sc + 3), eyn = st_ldy(k, sc + 3);
     const float dn = st_data(k, c, sc + 1);
-    Pb[C2][k.w][k.lane] = S.P[C2];
+    Pb[C2][k.w + 1][k.lane] = S.P[C2];
     const float p0 = S.P[C], p1 = S.P[C1], p2 = S.P[C2];
     float L1 = __shfl_up_sync(0xffffffffu, p1, 1);
     float R1 = __shfl_down_sync(0xffffffffu, p1, 1);
     if (k.need_x && k.xoff < 0) L1 = S.EX[C1];
     if (k.need_x && k.xoff > 0) R1 = S.EX[C1];
-    const float U1 = k.w > 0 ? Pb[C1][k.w - 1][k.lane] : S.EY[C1];
-    const float D1 = k.w < ST_WARPS - 1 ? Pb[C1][k.w + 1][k.lane] : S.EY[C1];
+    const float U1 = k.w > 0 ? Pb[C1][k.w][k.lane] : S.EY[C1];
+    const float D1 = k.w < ST_WARPS - 1 ? Pb[C1][k.w + 2][k.lane] : S.EY[C1];
     GN gn = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (k.in && pn >= 0 && pn < k.L) {
         const float xl = (k.x > 0 || k.ref) ? L1 : p1;
@@ -962,46 +967,63 @@ __device__ __forceinline__ void stencil_step(const StencilCtx &k, const StepCons
     S.DT[C1] = dn;  // plane rel+1
 }
 
-// x/y-interior step: the same arithmetic as stencil_step for blocks whose
-// threads and neighbour loads all lie inside the volume away from the x and
-// y faces (no x = 0, y = 0 or last-index rule applies, every thread is
-// inside).  The per-thread boundary selects and bounds tests drop out; the z
-// rules depend only on the plane, so they stay as block-uniform tests; phi is
-// read and written through pointers that advance one plane per step.
-// INSIDE: the block's outputs all lie in the valid region (blk_inside), and
-// dp walks the thread's column of the data factor one plane per step.
+// Border-band data factor (f_out = f_in = 30/30 = 1) from the image at ip.
+__device__ __forceinline__ float border_data(const unsigned char *ip, const StepConst &c) {
+    const float I = c.img_f32 ? __ldg(reinterpret_cast<const float *>(ip)) : (float)__ldg(ip);
+    const float d = __fsub_rn(I, 1.0f);
+    const float e = __fmul_rn(d, d);
+    return data_factor(e, e, c.l1, c.l2, c.lam_equal != 0);
+}
+
+// Fast step: the same arithmetic as stencil_step with every boundary rule
+// that depends on the thread's voxel decided once per thread (rows of the
+// y neighbours in the shared rings, x face flags) and phi, the output, the
+// data factor and the image read through pointers that advance one plane per
+// step.  The two extra rows of Pb hold the y neighbours of the halo rows.
+// In the reference boundary mode, lane 0 of a block at x = 0 carries the
+// previous linear element of lane 1's voxel, (W - 1, y - 1): its phi and its
+// normalised gradient reach lane 1 through the ordinary shuffles.
+// INSIDE: every output of the block lies in the valid region (blk_inside).
 // EDGE: the step may meet a z rule or an end of the block's plane range
 // (steps of the first and last groups of three, and groups near the first or
 // last plane of the volume); otherwise every plane test is known to pass.
+// FACE: the block touches an x or y face (per-thread rules apply).
 // acc collects out * 0, which is NaN once any output is not finite.
-template <int C, Arith A, bool INSIDE, bool EDGE>
-__device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepConst &c, StencilState &S, int sc,
-                                                const float *&pp, float *&op, const float *&dp,
-                                                float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
-                                                float &acc) {
+template <int C, Arith A, bool INSIDE, bool EDGE, bool FACE>
+__device__ __forceinline__ void stencil_step_f(const StencilCtx &k, const StepConst &c, StencilState &S, int sc,
+                                               const float *&pp, float *&op, const float *&dp,
+                                               const unsigned char *&ip, float (*Pb)[ST_WARPS + 2][32],
+                                               float2 (*Gb)[ST_WARPS][32], float &acc) {
     constexpr int C1 = (C + 1) % 3, C2 = (C + 2) % 3;
     float p3 = 0.0f, exn = 0.0f, eyn = 0.0f;  // plane sc + 3
     if (!EDGE || sc + 3 < k.L) {
-        p3 = __ldg(pp);
+        if (!FACE || k.in) p3 = __ldg(pp);
         if (k.need_x) exn = __ldg(pp + k.xoff);
         if (k.need_y) eyn = __ldg(pp + k.yoff);
     }
-    float dn;  // data factor of plane sc + 1
-    if constexpr (INSIDE) {
-        dn = (k.outp && (!EDGE || (sc + 1 >= k.z0 && sc + 1 < k.z1))) ? __ldg(dp) : 0.0f;
-        dp += k.dplane;
-    } else {
-        dn = st_data(k, c, sc + 1);
+    float dn = 0.0f;  // data factor of plane sc + 1
+    const int pd = sc + 1;
+    if (k.outp && (!EDGE || (pd >= k.z0 && pd < k.z1))) {
+        if (INSIDE || (k.inside_xy && pd >= k.r && pd < k.L - k.r)) dn = __ldg(dp);
+        else dn = border_data(ip, c);
     }
+    dp += k.dplane;
+    if (!INSIDE) ip += k.WH * (c.img_f32 ? 4 : 1);
     pp += k.WH;
-    Pb[C2][k.w][k.lane] = S.P[C2];
+    Pb[C2][k.w + 1][k.lane] = S.P[C2];
+    if (k.w == 0) Pb[C2][0][k.lane] = S.EY[C2];
+    if (k.w == ST_WARPS - 1) Pb[C2][ST_WARPS + 1][k.lane] = S.EY[C2];
     const float p0 = S.P[C], p1 = S.P[C1], p2 = S.P[C2];
     float L1 = __shfl_up_sync(0xffffffffu, p1, 1);
     float R1 = __shfl_down_sync(0xffffffffu, p1, 1);
     if (k.lane == 0) L1 = S.EX[C1];
     if (k.lane == 31) R1 = S.EX[C1];
-    const float U1 = k.w > 0 ? Pb[C1][k.w - 1][k.lane] : S.EY[C1];
-    const float D1 = k.w < ST_WARPS - 1 ? Pb[C1][k.w + 1][k.lane] : S.EY[C1];
+    if (FACE) {
+        if (k.xl_self) L1 = p1;
+        if (k.xr_self) R1 = p1;
+    }
+    const float U1 = Pb[C1][k.urow][k.lane];
+    const float D1 = Pb[C1][k.drow][k.lane];
     // gradient of plane pn = sc + 1 (z rules at the first and last plane; a
     // plane outside the volume gets a value that no output reads)
     const int pn = sc + 1;
@@ -1010,10 +1032,20 @@ __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepC
     Gb[C1][k.w][k.lane] = make_float2(gn.ny, gn.gy);
     __syncthreads();
     const GN4 &gc = S.G[C];
-    const float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
-    const float gxL = __shfl_up_sync(0xffffffffu, gc.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gc.gx, 1);
+    float nxL = __shfl_up_sync(0xffffffffu, gc.nx, 1), nxR = __shfl_down_sync(0xffffffffu, gc.nx, 1);
+    float gxL = __shfl_up_sync(0xffffffffu, gc.gx, 1), gxR = __shfl_down_sync(0xffffffffu, gc.gx, 1);
     if ((!EDGE || sc >= k.z0) && k.outp) {
-        const float2 yl2 = Gb[C][k.w - 1][k.lane], yr2 = Gb[C][k.w + 1][k.lane];
+        if (FACE) {
+            if (k.xl_self) {
+                nxL = gc.nx;
+                gxL = gc.gx;
+            }
+            if (k.xr_self) {
+                nxR = gc.nx;
+                gxR = gc.gx;
+            }
+        }
+        const float2 yl2 = Gb[C][k.gwl][k.lane], yr2 = Gb[C][k.gwr][k.lane];
         const float nyl = yl2.x, nyr = yr2.x, gyl = yl2.y, gyr = yr2.y;
         const GN4 &gp = S.G[C2];
         const bool zlo = !EDGE || sc > 0, zhi = !EDGE || sc < k.L - 1;
@@ -1033,25 +1065,25 @@ __device__ __forceinline__ void stencil_step_in(const StencilCtx &k, const StepC
     S.DT[C1] = dn;
 }
 
-// The steps of an x/y-interior block in groups of three (one per ring
+// The steps of a block on the fast path in groups of three (one per ring
 // slot); groups that can meet no z rule and no end of the plane range run
 // without the plane tests.
-template <Arith A, bool INSIDE>
-__device__ __forceinline__ void stencil_planes_in(const StencilCtx &k, const StepConst &c, StencilState &S, int count,
-                                                  const float *&pp, float *&op, const float *&dp,
-                                                  float (*Pb)[ST_WARPS][32], float2 (*Gb)[ST_WARPS][32],
-                                                  float &acc) {
+template <Arith A, bool INSIDE, bool FACE>
+__device__ __forceinline__ void stencil_planes_f(const StencilCtx &k, const StepConst &c, StencilState &S, int count,
+                                                 const float *&pp, float *&op, const float *&dp,
+                                                 const unsigned char *&ip, float (*Pb)[ST_WARPS + 2][32],
+                                                 float2 (*Gb)[ST_WARPS][32], float &acc) {
     for (int i = 0; i < count; i += 3) {
         const int sc = k.first + i;
         const bool edge = i == 0 || i + 3 >= count || sc <= 0 || sc + 5 >= k.L;
         if (edge) {
-            stencil_step_in<0, A, INSIDE, true>(k, c, S, sc, pp, op, dp, Pb, Gb, acc);
-            if (i + 1 < count) stencil_step_in<1, A, INSIDE, true>(k, c, S, sc + 1, pp, op, dp, Pb, Gb, acc);
-            if (i + 2 < count) stencil_step_in<2, A, INSIDE, true>(k, c, S, sc + 2, pp, op, dp, Pb, Gb, acc);
+            stencil_step_f<0, A, INSIDE, true, FACE>(k, c, S, sc, pp, op, dp, ip, Pb, Gb, acc);
+            if (i + 1 < count) stencil_step_f<1, A, INSIDE, true, FACE>(k, c, S, sc + 1, pp, op, dp, ip, Pb, Gb, acc);
+            if (i + 2 < count) stencil_step_f<2, A, INSIDE, true, FACE>(k, c, S, sc + 2, pp, op, dp, ip, Pb, Gb, acc);
         } else {
-            stencil_step_in<0, A, INSIDE, false>(k, c, S, sc, pp, op, dp, Pb, Gb, acc);
-            stencil_step_in<1, A, INSIDE, false>(k, c, S, sc + 1, pp, op, dp, Pb, Gb, acc);
-            stencil_step_in<2, A, INSIDE, false>(k, c, S, sc + 2, pp, op, dp, Pb, Gb, acc);
+            stencil_step_f<0, A, INSIDE, false, FACE>(k, c, S, sc, pp, op, dp, ip, Pb, Gb, acc);
+            stencil_step_f<1, A, INSIDE, false, FACE>(k, c, S, sc + 1, pp, op, dp, ip, Pb, Gb, acc);
+            stencil_step_f<2, A, INSIDE, false, FACE>(k, c, S, sc + 2, pp, op, dp, ip, Pb, Gb, acc);
         }
     }
 }
@@ -1125,7 +1157,7 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
                                                                    const int *__restrict__ pre,
                                                                    const StepConst c, int parity,
                                                                    unsigned *__restrict__ flag, DebugOut dbg) {
-    __shared__ float Pb[3][ST_WARPS][32];
+    __shared__ float Pb[3][ST_WARPS + 2][32];
     __shared__ float2 Gb[3][ST_WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;
@@ -1144,6 +1176,12 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     const int ty = t % nty;
     const int tz = t / nty;
     const int x0 = tx * ST_OX, y0 = ty * ST_OY;
+    k.ref = c.boundary == 0;
+    // Every block takes the fast path but in the debug step and, in the
+    // reference mode, the blocks at x = 0 that hold row 0 (where the previous
+    // linear element of voxel (0, 0) lies in the previous plane).
+    const bool fast = !DEBUG && !(k.ref && x0 == 0 && y0 < 2);
+    const bool prev_lane = fast && k.ref && x0 == 0 && lane == 0;
     k.x = x0 - 1 + lane;
     k.y = y0 - 1 + w;
     k.w = w;
@@ -1151,36 +1189,43 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     k.z0 = tz * c.zc;
     k.z1 = min(k.z0 + c.zc, k.L);
     k.first = k.z0 - 2;
-    k.in = k.x >= 0 && k.x < k.W && k.y >= 0 && k.y < k.H;
-    k.outp = k.in && lane >= 1 && lane <= ST_OX && w >= 1 && w <= ST_OY;
-    k.ref = c.boundary == 0;
+    // the thread's voxel: lane 0 at x = 0 may carry (W - 1, y - 1)
+    const int ex = prev_lane ? k.W - 1 : k.x, ey = prev_lane ? k.y - 1 : k.y;
+    k.in = ex >= 0 && ex < k.W && ey >= 0 && ey < k.H;
+    k.outp = k.in && !prev_lane && lane >= 1 && lane <= ST_OX && w >= 1 && w <= ST_OY;
     k.WH = (size_t)k.W * k.H;
-    k.col = k.in ? (size_t)k.y * k.W + k.x : 0;
+    k.col = k.in ? (size_t)ey * k.W + ex : 0;
     k.phi = (parity ? s.phi[1] : s.phi[0]) + k.col;
     k.phi_out = parity ? s.phi[0] : s.phi[1];
     const bool valid = s.Wv > 0;
     const int r = k.r;
-    k.inside_xy = valid && k.x >= r && k.x < k.W - r && k.y >= r && k.y < k.H - r;
+    k.inside_xy = valid && ex >= r && ex < k.W - r && ey >= r && ey < k.H - r;
     k.blk_inside = valid && x0 >= r && x0 + ST_OX - 1 < k.W - r && y0 >= r && y0 + ST_OY - 1 < k.H - r &&
                    k.z0 >= r && k.z1 - 1 < k.L - r;
     k.dplane = (size_t)s.Wp * s.Hv;
-    k.dcol = k.inside_xy ? s.db + (size_t)(k.y - r) * s.Wp + (k.x - r) : s.db;
+    k.dcol = k.inside_xy ? s.db + (size_t)(ey - r) * s.Wp + (ex - r) : s.db;
     if (c.full_data) {  // every voxel's data factor comes from the box or expanded data-term kernels
         k.blk_inside = true;
         k.dplane = k.WH;
         k.dcol = s.db + 2 * (size_t)s.Wp * s.Hv * s.Lv + k.col + (size_t)r * k.WH;
     }
     // The shuffles and shared rows supply every neighbour except: x-1 for
-    // lane 0 and, in the reference mode, the previous linear element for
-    // x == 0 (both at linear offset -1); x+1 for lane 31; y-1 / y+1 for the
-    // halo rows.  Corner threads of the halo are never read.
+    // lane 0 (and, on the debug path, the previous linear element for x == 0
+    // in the reference mode), both at linear offset -1; x+1 for lane 31;
+    // y-1 / y+1 for the halo rows.  Corner threads of the halo are never read.
     const bool halo_row = w == 0 || w == ST_WARPS - 1;
     const bool halo_col = lane == 0 || lane == 31;
     k.need_x = k.in && !(halo_row && halo_col) &&
-               ((lane == 0) || (k.x == 0 && k.ref) || (lane == 31 && k.x + 1 < k.W));
+               ((lane == 0) || (!fast && k.x == 0 && k.ref) || (lane == 31 && ex + 1 < k.W));
     k.xoff = lane == 31 ? 1 : -1;
-    k.need_y = k.in && halo_row && !halo_col && (w == 0 ? k.y > 0 : k.y + 1 < k.H);
+    k.need_y = k.in && halo_row && !halo_col && (w == 0 ? ey > 0 : ey + 1 < k.H);
     k.yoff = w == 0 ? -(ptrdiff_t)k.W : (ptrdiff_t)k.W;
+    k.xl_self = !k.ref && ex == 0;
+    k.xr_self = ex == k.W - 1;
+    k.urow = ey > 0 ? w : w + 1;
+    k.drow = ey < k.H - 1 ? w + 2 : w + 1;
+    k.gwl = ey > 0 ? w - 1 : w;
+    k.gwr = ey < k.H - 1 ? w + 1 : w;
 
     StencilState S;
     const int sp = k.first;
@@ -1194,20 +1239,31 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 2) stencil_kernel(const SubVolD
     S.EX[0] = S.EY[0] = 0.0f;
     S.DT[0] = S.DT[1] = S.DT[2] = 0.0f;
     for (int i = 0; i < 3; ++i) S.G[i] = GN4{0.f, 0.f, 0.f, 0.f};
-    Pb[1][w][lane] = S.P[1];
+    Pb[1][w + 1][lane] = S.P[1];
+    if (w == 0) Pb[1][0][lane] = S.EY[1];
+    if (w == ST_WARPS - 1) Pb[1][ST_WARPS + 1][lane] = S.EY[1];
     __syncthreads();
     const int count = k.z1 - k.first;
-    // x/y-interior blocks: every thread and neighbour load inside, no x or y
-    // face rule.
-    const bool interior = !DEBUG && x0 >= 2 && x0 + 32 <= k.W && y0 >= 2 && y0 + ST_OY + 2 <= k.H;
-    if (interior) {
+    if (fast) {
         const float *pp = k.phi + (ptrdiff_t)(k.first + 3) * (ptrdiff_t)k.WH;
         float *op = k.phi_out + (ptrdiff_t)k.first * (ptrdiff_t)k.WH + (ptrdiff_t)k.col;
-        // plane first + 1 of the data column (read only from plane z0 on)
+        // plane first + 1 of the data column and of the image (read only
+        // from plane z0 on)
         const float *dp = k.dcol + ((ptrdiff_t)k.first + 1 - k.r) * (ptrdiff_t)k.dplane;
+        const ptrdiff_t esz = c.img_f32 ? 4 : 1;
+        const unsigned char *ip = static_cast<const unsigned char *>(s.img) +
+                                  ((ptrdiff_t)k.col + ((ptrdiff_t)k.first + 1) * (ptrdiff_t)k.WH) * esz;
+        // x/y-interior blocks: every thread and neighbour load inside, no x
+        // or y face rule
+        const bool face = !(x0 >= 2 && x0 + 32 <= k.W && y0 >= 2 && y0 + ST_OY + 2 <= k.H);
         float acc = 0.0f;
-        if (k.blk_inside) stencil_planes_in<A, true>(k, c, S, count, pp, op, dp, Pb, Gb, acc);
-        else stencil_planes_in<A, false>(k, c, S, count, pp, op, dp, Pb, Gb, acc);
+        if (face) {
+            if (k.blk_inside) stencil_planes_f<A, true, true>(k, c, S, count, pp, op, dp, ip, Pb, Gb, acc);
+            else stencil_planes_f<A, false, true>(k, c, S, count, pp, op, dp, ip, Pb, Gb, acc);
+        } else {
+            if (k.blk_inside) stencil_planes_f<A, true, false>(k, c, S, count, pp, op, dp, ip, Pb, Gb, acc);
+            else stencil_planes_f<A, false, false>(k, c, S, count, pp, op, dp, ip, Pb, Gb, acc);
+        }
         if (!isfinite(acc)) atomicOr(flag, kFlagNonFinite);
         return;
     }
