@@ -122,111 +122,116 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
     const int sv = find_sv(pre, c.nsv, b);
     const SubVolDev s = svs[sv];
     int t = b - __ldg(pre + sv);
-    const int ntx = (s.Wv + XT - 1) / XT, nty = (s.H + XP_ROWS - 1) / XP_ROWS;
+    const int ntx = (s.Wv + XT - 1) / XT, nty = (s.H + XP_ROWS * XP_RPW - 1) / (XP_ROWS * XP_RPW);
     const int tx = t % ntx;
     t /= ntx;
     const int ty = t % nty;
     const int z = t / nty;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = ty * XP_ROWS + warp;
     float2 *taps_s = reinterpret_cast<float2 *>(sm4 + XP_ROWS * span);  // MAXK pairs, then the pair-0 stages
     if (K == 0) {
         for (int i = threadIdx.x; i < k; i += blockDim.x) taps_s[i] = c.taps2[i];
         __syncthreads();
     }
-    if (y >= s.H) return;
     float4 *in = sm4 + warp * span;
     const int x0 = tx * XT;
-    const size_t row = ((size_t)z * s.H + y) * s.W;
-    const float *phi = (parity ? s.phi[1] : s.phi[0]) + row;
-    if constexpr (K > 0) {
-        // all of the lane's loads first, so that they are in flight together
-        constexpr int NE = (XT + K - 1 + 31) / 32;
-        float ph[NE], im[NE];
+    // XP_RPW rows per warp, XP_ROWS apart: the block setup above is paid
+    // once per XP_RPW row segments
+    for (int j = 0; j < XP_RPW; ++j) {
+        const int y = (ty * XP_RPW + j) * XP_ROWS + warp;
+        if (y >= s.H) break;
+        if (j > 0) __syncwarp();  // the previous row's stores have read the slab
+        const size_t row = ((size_t)z * s.H + y) * s.W;
+        const float *phi = (parity ? s.phi[1] : s.phi[0]) + row;
+        if constexpr (K > 0) {
+            // all of the lane's loads first, so that they are in flight together
+            constexpr int NE = (XT + K - 1 + 31) / 32;
+            float ph[NE], im[NE];
 #pragma unroll
-        for (int q = 0; q < NE; ++q) {
-            const int e = lane + 32 * q, x = x0 + e;
-            const bool ok = e < span && x < s.W;
-            ph[q] = ok ? __ldg(phi + x) : 0.0f;
-            im[q] = ok ? load_img(s.img, row + x, c.img_f32) : 0.0f;
-        }
+            for (int q = 0; q < NE; ++q) {
+                const int e = lane + 32 * q, x = x0 + e;
+                const bool ok = e < span && x < s.W;
+                ph[q] = ok ? __ldg(phi + x) : 0.0f;
+                im[q] = ok ? load_img(s.img, row + x, c.img_f32) : 0.0f;
+            }
 #pragma unroll
-        for (int q = 0; q < NE; ++q) {
-            const int e = lane + 32 * q;
-            if (e < span) {
+            for (int q = 0; q < NE; ++q) {
+                const int e = lane + 32 * q;
+                if (e < span) {
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (x0 + e < s.W) {
+                        const float h = heaviside<A>(ph[q], c.eps);
+                        const float hi = __fsub_rn(1.0f, h);
+                        v = make_float4(h, hi, __fmul_rn(im[q], h), __fmul_rn(im[q], hi));
+                    }
+                    in[e] = v;
+                }
+            }
+        } else {
+            for (int e = lane; e < span; e += 32) {
+                const int x = x0 + e;
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (x0 + e < s.W) {
-                    const float h = heaviside<A>(ph[q], c.eps);
+                if (x < s.W) {
+                    const float h = heaviside<A>(__ldg(phi + x), c.eps);
+                    const float I = load_img(s.img, row + x, c.img_f32);
                     const float hi = __fsub_rn(1.0f, h);
-                    v = make_float4(h, hi, __fmul_rn(im[q], h), __fmul_rn(im[q], hi));
+                    v = make_float4(h, hi, __fmul_rn(I, h), __fmul_rn(I, hi));
                 }
                 in[e] = v;
             }
         }
-    } else {
-        for (int e = lane; e < span; e += 32) {
-            const int x = x0 + e;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (x < s.W) {
-                const float h = heaviside<A>(__ldg(phi + x), c.eps);
-                const float I = load_img(s.img, row + x, c.img_f32);
-                const float hi = __fsub_rn(1.0f, h);
-                v = make_float4(h, hi, __fmul_rn(I, h), __fmul_rn(I, hi));
+        __syncwarp();
+        // Pair 0 (H, 1-H) is staged in its own slab, pair 1 (I H, I (1-H)) in
+        // the input slab once every lane has finished reading it.
+        float *st01 = reinterpret_cast<float *>(sm4 + XP_ROWS * span) + 2 * MAXK + warp * 2 * XT;
+        float *st23 = reinterpret_cast<float *>(in);
+        const float2 *src = reinterpret_cast<const float2 *>(in + XB * lane);
+        float2 acc[XB];
+        if constexpr (K > 0) {
+            // two float2 pair planes: each pair's results are staged as float2
+            // and written as float4 (two columns)
+            float2 *s01 = reinterpret_cast<float2 *>(st01), *s23 = reinterpret_cast<float2 *>(st23);
+            xconv_pair<K, XB>(src, c, taps_s, k, acc);
+#pragma unroll
+            for (int m = 0; m < XB; ++m) s01[XB * lane + m] = acc[m];
+            xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
+            __syncwarp();
+#pragma unroll
+            for (int m = 0; m < XB; ++m) s23[XB * lane + m] = acc[m];
+            __syncwarp();
+            const size_t pstride = (size_t)s.Wp * s.H * s.L;
+            const size_t orow = ((size_t)z * s.H + y) * s.Wp;
+#pragma unroll
+            for (int pp = 0; pp < 2; ++pp) {
+                const float4 *sf = reinterpret_cast<const float4 *>(pp ? s23 : s01);
+                float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(s.xb) + pp * pstride + orow + x0);
+                for (int e = lane; e < XT / 2; e += 32)
+                    if (x0 + 2 * e < s.Wv) dst[e] = sf[e];
             }
-            in[e] = v;
-        }
-    }
-    __syncwarp();
-    // Pair 0 (H, 1-H) is staged in its own slab, pair 1 (I H, I (1-H)) in
-    // the input slab once every lane has finished reading it.
-    float *st01 = reinterpret_cast<float *>(sm4 + XP_ROWS * span) + 2 * MAXK + warp * 2 * XT;
-    float *st23 = reinterpret_cast<float *>(in);
-    const float2 *src = reinterpret_cast<const float2 *>(in + XB * lane);
-    float2 acc[XB];
-    if constexpr (K > 0) {
-        // two float2 pair planes: each pair's results are staged as float2
-        // and written as float4 (two columns)
-        float2 *s01 = reinterpret_cast<float2 *>(st01), *s23 = reinterpret_cast<float2 *>(st23);
-        xconv_pair<K, XB>(src, c, taps_s, k, acc);
+        } else {
+            xconv_pair<K, XB>(src, c, taps_s, k, acc);
 #pragma unroll
-        for (int m = 0; m < XB; ++m) s01[XB * lane + m] = acc[m];
-        xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
-        __syncwarp();
+            for (int m = 0; m < XB; ++m) {
+                st01[XB * lane + m] = acc[m].x;
+                st01[XT + XB * lane + m] = acc[m].y;
+            }
+            xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
+            __syncwarp();
 #pragma unroll
-        for (int m = 0; m < XB; ++m) s23[XB * lane + m] = acc[m];
-        __syncwarp();
-        const size_t pstride = (size_t)s.Wp * s.H * s.L;
-        const size_t orow = ((size_t)z * s.H + y) * s.Wp;
+            for (int m = 0; m < XB; ++m) {
+                st23[XB * lane + m] = acc[m].x;
+                st23[XT + XB * lane + m] = acc[m].y;
+            }
+            __syncwarp();
+            const size_t fstride = (size_t)s.Wp * s.H * s.L;
+            const size_t orow = ((size_t)z * s.H + y) * s.Wp;
 #pragma unroll
-        for (int pp = 0; pp < 2; ++pp) {
-            const float4 *sf = reinterpret_cast<const float4 *>(pp ? s23 : s01);
-            float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(s.xb) + pp * pstride + orow + x0);
-            for (int e = lane; e < XT / 2; e += 32)
-                if (x0 + 2 * e < s.Wv) dst[e] = sf[e];
-        }
-    } else {
-        xconv_pair<K, XB>(src, c, taps_s, k, acc);
-#pragma unroll
-        for (int m = 0; m < XB; ++m) {
-            st01[XB * lane + m] = acc[m].x;
-            st01[XT + XB * lane + m] = acc[m].y;
-        }
-        xconv_pair<K, XB>(src + 1, c, taps_s, k, acc);
-        __syncwarp();
-#pragma unroll
-        for (int m = 0; m < XB; ++m) {
-            st23[XB * lane + m] = acc[m].x;
-            st23[XT + XB * lane + m] = acc[m].y;
-        }
-        __syncwarp();
-        const size_t fstride = (size_t)s.Wp * s.H * s.L;
-        const size_t orow = ((size_t)z * s.H + y) * s.Wp;
-#pragma unroll
-        for (int f = 0; f < 4; ++f) {
-            const float4 *sf = reinterpret_cast<const float4 *>((f < 2 ? st01 : st23) + (f & 1) * XT);
-            float4 *dst = reinterpret_cast<float4 *>(s.xb + f * fstride + orow + x0);
-            for (int e = lane; e < XT / 4; e += 32)
-                if (x0 + 4 * e < s.Wv) dst[e] = sf[e];
+            for (int f = 0; f < 4; ++f) {
+                const float4 *sf = reinterpret_cast<const float4 *>((f < 2 ? st01 : st23) + (f & 1) * XT);
+                float4 *dst = reinterpret_cast<float4 *>(s.xb + f * fstride + orow + x0);
+                for (int e = lane; e < XT / 4; e += 32)
+                    if (x0 + 4 * e < s.Wv) dst[e] = sf[e];
+            }
         }
     }
 }

@@ -134,7 +134,7 @@ bool encode_pair_map(void *out, const SubVolDev &d) {
 void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NPRE]) {
     const bool valid = d.Wv > 0;
     const int xt = 32 * sh.xb_w, zc = sh.zc;
-    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS - 1) / XP_ROWS) * d.L : 0;
+    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS * XP_RPW - 1) / (XP_ROWS * XP_RPW)) * d.L : 0;
     if (!valid) tiles[1] = 0;
     else if (kspec == 0) tiles[1] = ((d.Wv + YB_TX - 1) / YB_TX) * ((d.Hv + YB_YB - 1) / YB_YB) * 4 * d.L;
     else tiles[1] = ((d.Wv + YP_COLS - 1) / YP_COLS) * 2 * d.L;  // one column of one pair per thread
