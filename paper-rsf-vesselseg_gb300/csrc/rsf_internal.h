@@ -10,7 +10,7 @@ constexpr int MAXK = 128;  // largest supported tap count (sigma up to ~18)
 
 // Kernel tilings (the launchers derive tile counts from them).
 constexpr int XP_ROWS = 4;     // x-pass: warps per block
-constexpr int XP_RPW = 4;      // x-pass: rows per warp (XP_ROWS apart)
+constexpr int XP_RPW = 8;      // x-pass: rows per warp (XP_ROWS apart)
 constexpr int YP_COLS = 128;   // y-pass: columns per block (one column of one pair per thread)
 constexpr int YB_TX = 128;     // generic y-pass: columns per block
 constexpr int YB_YB = 16;      // generic y-pass: outputs per thread along y
