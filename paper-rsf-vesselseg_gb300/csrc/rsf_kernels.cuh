@@ -329,9 +329,9 @@ __device__ __forceinline__ void stream_axis(const Ring &rg, const StepConst &c, 
 }
 
 // Ring with compile-time slots, for tap counts that are a multiple of the
-// ring depth RD (21 and 35 with RD = 7).  Blocks of K elements start at
-// multiples of K, so element base + j sits in slot j % RD, a constant of the
-// unrolled block; the global addresses advance by one stride per element
+// ring depth RD (21 and 35 with RD = 7, 29 with RD = 29).  Blocks of K
+// elements start at multiples of K, so element base + j sits in slot j % RD,
+// a constant of the unrolled block; the global addresses advance by one stride per element
 // instead of being recomputed.  Same commit-group protocol as Ring: element
 // i is group i; iteration i refills the slot of element i-1 with element
 // i-1+RD and then waits until at most RD-1 groups are pending.
@@ -412,7 +412,10 @@ __device__ __forceinline__ void stream_axis_c(RingC<RD> &rg, const StepConst &c,
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-__host__ __device__ constexpr int ring_depth(int K) { return K % 7 == 0 ? 7 : RING; }
+// Depth of the compile-time ring of a specialised tap count: 7 for 21 and
+// 35; 29 (prime) takes a ring as deep as its taps (44.5 KB of shared memory
+// per block, within what its registers already allow per SM).
+__host__ __device__ constexpr int ring_depth(int K) { return K % 7 == 0 ? 7 : K == 29 ? 29 : RING; }
 
 // Register-blocked version for a tap count known only at run time: NB
 // consecutive outputs per call, same accumulation order.
@@ -557,8 +560,9 @@ __device__ __forceinline__ void zpass_body(const SubVolDev &s, const StepConst &
                                    2 * ((size_t)y * s.Wp + (act ? x + (f & 1) : 0))
                              : s.yb + f * ((size_t)s.Wp * s.Hv * s.L) + (size_t)y * s.Wp + (act ? x : 0);
     const size_t pstride = (PAIRS ? 2 : 1) * (size_t)s.Wp * s.Hv;
-    __shared__ float2 ring[RING * ZP_PAIRS * 4];
-    __shared__ unsigned iring[RING * ZP_PAIRS * 4];
+    constexpr int RS = ring_depth(K) > RING ? ring_depth(K) : RING;
+    __shared__ float2 ring[RS * ZP_PAIRS * 4];
+    __shared__ unsigned iring[RS * ZP_PAIRS * 4];
     // The image at this lane's voxel of output plane o (input plane o + r)
     // rides in the ring with element i = o + 2r.
     const int xc = zlane_col<PAIRS>(x, f);
