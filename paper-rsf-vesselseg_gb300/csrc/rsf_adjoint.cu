@@ -87,10 +87,11 @@ __device__ __forceinline__ BlockVol block_vol(const int *__restrict__ pre, int n
     return {lo, (long long)(b - __ldg(pre + lo))};
 }
 
-// The stencil kernels run on blocks of 32 x 8 voxels of one z plane (w,
+// The stencil kernels run on blocks of 32 x 8 voxels of kWZ planes (w,
 // gather) or of kPointZ planes (pointwise terms).
 constexpr int kBX = 32, kBY = 8;
 constexpr int kPointZ = 16;
+constexpr int kWZ = 8;  // planes per block of adj_w and adj_gather
 
 struct Geo {
     int W, H, L, boundary;
@@ -485,9 +486,10 @@ __global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__r
     const float *kb = a.xs + 2 * N, *u = a.u;
     auto kbar = [&](long long m) { return kb[m]; };
     auto lbar = [&](long long m) { return u[m] * c.dt * c.mu; };
-    const Col cl = col_of(a, bv.t, 1);
-    const int x = cl.x, y = cl.y, z = cl.z0;
-    if (x < a.W && y < a.H) {
+    const Col cl = col_of(a, bv.t, kWZ);
+    const int x = cl.x, y = cl.y;
+    const int z1 = min(cl.z0 + kWZ, a.L);
+    for (int z = cl.z0; z < z1 && x < a.W && y < a.H; ++z) {
         float *gxa = a.xs, *gya = a.xs + N, *gza = a.ys;
         const float *nx = a.ys + N, *ny = a.ys + 2 * N, *nz = a.ys + 3 * N;
         const long long i = ((long long)z * a.H + y) * a.W + x;
@@ -518,9 +520,10 @@ __global__ void __launch_bounds__(kBX * kBY) adj_gather(AdjConst c, const AdjVol
     auto vx = [&](long long m) { return wx[m]; };
     auto vy = [&](long long m) { return wy[m]; };
     auto vz = [&](long long m) { return wz[m]; };
-    const Col cl = col_of(a, bv.t, 1);
-    const int x = cl.x, y = cl.y, z = cl.z0;
-    if (x < a.W && y < a.H) {
+    const Col cl = col_of(a, bv.t, kWZ);
+    const int x = cl.x, y = cl.y;
+    const int z1 = min(cl.z0 + kWZ, a.L);
+    for (int z = cl.z0; z < z1 && x < a.W && y < a.H; ++z) {
         const long long i = ((long long)z * a.H + y) * a.W + x;
         const float v = a.out[i] + (dT_x(g, i, x, N, vx) + dT_axis(i, y, a.H, a.W, vy) + dT_axis(i, z, a.L, plane, vz));
         a.out[i] = v;
@@ -551,8 +554,8 @@ void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]) {
     t[ADJ_TX] = cdiv(N, kThreads);
     t[ADJ_NRM] = cdiv(N, kThreads);
     t[ADJ_PT] = bxy * cdiv(v.L, kPointZ);
-    t[ADJ_W] = bxy * v.L;
-    t[ADJ_G] = bxy * v.L;
+    t[ADJ_W] = bxy * cdiv(v.L, kWZ);
+    t[ADJ_G] = bxy * cdiv(v.L, kWZ);
     for (int j = 0; j < NADJ; j++) tiles[j] = t[j] > 0x7fffffffLL ? -1 : (int)t[j];
 }
 

@@ -364,7 +364,10 @@ rsf_status prepare(rsf_workspace *ws, const rsf_subvol *svs, int32_t n, int k, i
         whl[3 * i + 2] = (int)svs[i].L;
     }
     *shape = rsf::choose_shape(whl.data(), n, k, kspec, gauss);
-    if (ws->force_xb) shape->xb_w = ws->force_xb;
+    if (ws->force_xb) {
+        shape->xb_w = ws->force_xb;
+        shape->xrpw = rsf::choose_xrpw(whl.data(), n, k, shape->xb_w);
+    }
     if (ws->force_zc) shape->zc = ws->force_zc;
     if (ws->force_zt >= 0) shape->zt = ws->force_zt && rsf::tma_z(kspec) && rsf::tensor_maps_available() ? 1 : 0;
     const int n1 = n + 1;
@@ -440,6 +443,7 @@ StepConst make_const(const rsf_params *p, int k, const float *taps, rsf_dtype dt
     c.img_f32 = dtype == RSF_F32;
     c.nsv = n;
     c.xb_w = sh.xb_w;
+    c.xrpw = sh.xrpw;
     c.pairs = sh.pairs;
     c.zc = sh.zc;
     c.ymaps = sh.zt ? maps : nullptr;

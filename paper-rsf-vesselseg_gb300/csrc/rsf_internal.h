@@ -10,7 +10,7 @@ constexpr int MAXK = 128;  // largest supported tap count (sigma up to ~18)
 
 // Kernel tilings (the launchers derive tile counts from them).
 constexpr int XP_ROWS = 4;     // x-pass: warps per block
-constexpr int XP_RPW = 8;      // x-pass: rows per warp (XP_ROWS apart)
+constexpr int XP_RPW = 8;      // x-pass: largest rows per warp (XP_ROWS apart; chosen per launch)
 constexpr int YP_COLS = 128;   // y-pass: columns per block (one column of one pair per thread)
 constexpr int YB_TX = 128;     // generic y-pass: columns per block
 constexpr int YB_YB = 16;      // generic y-pass: outputs per thread along y
@@ -59,6 +59,7 @@ struct StepConst {
     int img_f32;    // 1: image is float32, 0: uint8
     int nsv;        // number of sub-volumes in the table
     int xb_w;       // x-pass outputs per lane for this launch
+    int xrpw;       // x-pass rows per warp for this launch
     int pairs;      // 1: x/y fields in float2 pair planes (specialised tap counts)
     int zc;         // stencil planes per block for this launch
     int box;        // e-term box radius (int)sigma2; 0: e = (I - f)^2
@@ -112,6 +113,7 @@ constexpr int MAX_BOX = 8;  // largest e-term box radius
 // Per-launch tile shapes of a batch.
 struct LaunchShape {
     int xb_w;   // x-pass outputs per lane
+    int xrpw;   // x-pass rows per warp (1, 2, 4 or XP_RPW)
     int pairs;  // 1: x/y fields in float2 pair planes (specialised tap counts)
     int zt;     // 1: the z-pass loads planes with TMA (needs a map per sub-volume)
     int zc;     // stencil planes per block
@@ -122,6 +124,9 @@ LaunchShape choose_shape(const int *whl, int n, int k, int kspec, int gauss = 0)
 // Blocks each kernel needs for one sub-volume (kspec: kernel_k()).
 void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NPRE]);
 int choose_xb(const int *Wv, int n);
+// Rows per warp of the x-pass: the most (up to XP_RPW) that still give
+// every SM several blocks.
+int choose_xrpw(const int *whl, int n, int k, int xb_w);
 int choose_zc(const int *whl, int n);  // whl: W, H, L of each sub-volume
 void valid_extents(int W, int H, int L, int k, int &Wv, int &Hv, int &Lv, int &Wp);
 

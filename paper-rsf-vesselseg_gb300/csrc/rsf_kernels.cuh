@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
     const int sv = find_sv(pre, c.nsv, b);
     const SubVolDev s = svs[sv];
     int t = b - __ldg(pre + sv);
-    const int ntx = (s.Wv + XT - 1) / XT, nty = (s.H + XP_ROWS * XP_RPW - 1) / (XP_ROWS * XP_RPW);
+    const int ntx = (s.Wv + XT - 1) / XT, nty = (s.H + XP_ROWS * c.xrpw - 1) / (XP_ROWS * c.xrpw);
     const int tx = t % ntx;
     t /= ntx;
     const int ty = t % nty;
@@ -135,10 +135,10 @@ __global__ void __launch_bounds__(XP_ROWS * 32) xpass_kernel(const SubVolDev *__
     }
     float4 *in = sm4 + warp * span;
     const int x0 = tx * XT;
-    // XP_RPW rows per warp, XP_ROWS apart: the block setup above is paid
-    // once per XP_RPW row segments
-    for (int j = 0; j < XP_RPW; ++j) {
-        const int y = (ty * XP_RPW + j) * XP_ROWS + warp;
+    // c.xrpw rows per warp, XP_ROWS apart: the block setup above is paid
+    // once per c.xrpw row segments
+    for (int j = 0; j < c.xrpw; ++j) {
+        const int y = (ty * c.xrpw + j) * XP_ROWS + warp;
         if (y >= s.H) break;
         if (j > 0) __syncwarp();  // the previous row's stores have read the slab
         const size_t row = ((size_t)z * s.H + y) * s.W;

@@ -162,6 +162,7 @@ extern "C" rsf_status rsf_evolve_noalloc(const rsf_params *p, const void *image,
     c.img_f32 = dtype == RSF_F32;
     c.nsv = 1;
     c.xb_w = sh.xb_w;
+    c.xrpw = sh.xrpw;
     c.pairs = sh.pairs;
     c.zc = sh.zc;
     alignas(64) unsigned char map[rsf::TMAP_BYTES];

@@ -67,6 +67,24 @@ int choose_zc(const int *whl, int n) {
     return blocks >= 4LL * 2 * sm_count() ? ST_ZC : ST_ZC / 2;
 }
 
+int choose_xrpw(const int *whl, int n, int k, int xb_w) {
+    const int xt = 32 * xb_w;
+    const long long want = 8LL * sm_count();
+    int rpw = XP_RPW;
+    for (; rpw > 1; rpw /= 2) {
+        long long blocks = 0;
+        for (int i = 0; i < n; i++) {
+            int Wv, Hv, Lv, Wp;
+            valid_extents(whl[3 * i], whl[3 * i + 1], whl[3 * i + 2], k, Wv, Hv, Lv, Wp);
+            if (Wv > 0)
+                blocks += (long long)((Wv + xt - 1) / xt) * ((whl[3 * i + 1] + XP_ROWS * rpw - 1) / (XP_ROWS * rpw)) *
+                          whl[3 * i + 2];
+        }
+        if (blocks >= want) break;
+    }
+    return rpw;
+}
+
 LaunchShape choose_shape(const int *whl, int n, int k, int kspec, int gauss) {
     LaunchShape sh;
     std::vector<int> wv((size_t)n);
@@ -76,6 +94,7 @@ LaunchShape choose_shape(const int *whl, int n, int k, int kspec, int gauss) {
         wv[(size_t)i] = Wv;
     }
     sh.xb_w = choose_xb(wv.data(), n);
+    sh.xrpw = choose_xrpw(whl, n, k, sh.xb_w);
     sh.pairs = kspec > 0 ? 1 : 0;
     sh.zt = tma_z(kspec) && tma_z_requested() && tensor_maps_available() ? 1 : 0;
     sh.zc = choose_zc(whl, n);
@@ -134,7 +153,8 @@ bool encode_pair_map(void *out, const SubVolDev &d) {
 void tile_counts(const SubVolDev &d, int kspec, const LaunchShape &sh, int tiles[NPRE]) {
     const bool valid = d.Wv > 0;
     const int xt = 32 * sh.xb_w, zc = sh.zc;
-    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + XP_ROWS * XP_RPW - 1) / (XP_ROWS * XP_RPW)) * d.L : 0;
+    const int xr = XP_ROWS * sh.xrpw;
+    tiles[0] = valid ? ((d.Wv + xt - 1) / xt) * ((d.H + xr - 1) / xr) * d.L : 0;
     if (!valid) tiles[1] = 0;
     else if (kspec == 0) tiles[1] = ((d.Wv + YB_TX - 1) / YB_TX) * ((d.Hv + YB_YB - 1) / YB_YB) * 4 * d.L;
     else tiles[1] = ((d.Wv + YP_COLS - 1) / YP_COLS) * 2 * d.L;  // one column of one pair per thread
