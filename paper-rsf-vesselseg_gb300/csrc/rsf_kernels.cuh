@@ -629,6 +629,26 @@ __global__ void __launch_bounds__(ZP_PAIRS * 4) zpass_kernel(const SubVolDev *__
         });
 }
 
+// The same z-pass bounded only to two resident blocks per SM.  For 35 taps
+// the default bounds hold it to 128 registers with a 56-byte spill of the 35
+// accumulator pairs; this one takes 164 registers without a spill (3 blocks
+// per SM instead of 4) and measured 1.43 against 1.89 ms per launch on a
+// 512^3 volume.
+template <int K, bool PAIRS>
+__global__ void __launch_bounds__(ZP_PAIRS * 4, 2) zpass_wide_kernel(const SubVolDev *__restrict__ svs,
+                                                                     const int *__restrict__ pre,
+                                                                     const StepConst c) {
+    const int b = blockIdx.x;
+    const int sv = find_sv(pre, c.nsv, b);
+    const SubVolDev s = svs[sv];
+    const DebugOut none = {nullptr, 0};
+    zpass_body<K, PAIRS>(
+        s, c, b - __ldg(pre + sv), [](int, int, bool) {},
+        [&](int f, int x, int y, int o, bool live, float I, float2 v) {
+            fits_and_data<PAIRS>(s, c, f, x, y, o, live, I, v, none, false);
+        });
+}
+
 // The adjoint's recompute of the fits (rsf_adjoint.cu): the forward z-pass
 // over pair planes, emitting at each valid voxel, instead of the data factor,
 //   e_out = (I - f_out)^2 and e_in at the full-volume index, and the pair
