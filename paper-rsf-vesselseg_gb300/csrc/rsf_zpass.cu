@@ -18,8 +18,11 @@ cudaError_t RSF_CAT(launch_zpass_, RSF_K)(const SubVolDev *svs, const int *pre, 
     const DebugOut none = {nullptr, 0};
 #if RSF_K > 0
     (void)dbg;
-    if (c.pairs && RSF_K == 35) zpass_wide_kernel<RSF_K, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c);
-    else if (c.pairs) zpass_kernel<RSF_K, false, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
+#if RSF_K == 35
+    if (c.pairs) zpass_wide_kernel<RSF_K, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c);
+#else
+    if (c.pairs) zpass_kernel<RSF_K, false, true><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
+#endif
     else zpass_kernel<RSF_K, false, false><<<blocks, ZP_PAIRS * 4, 0, st>>>(svs, pre, c, none);
 #else
     if (dbg) zpass_generic_kernel<true><<<blocks, ZB_TX, 0, st>>>(svs, pre, c, *dbg);
