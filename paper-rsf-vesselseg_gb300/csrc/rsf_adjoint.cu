@@ -160,6 +160,21 @@ __device__ __forceinline__ float dT_axis(long long j, int q, int n, long long st
     return acc;
 }
 
+// D_a^T v at a voxel that is neither first nor last along any axis: only
+// j - s (coefficient 1/2) and j + s (-1/2) read j, as in dT_x / dT_axis,
+// whose evaluation order this keeps (the coefficient-0 term of j itself
+// adds nothing to a finite sum).
+template <class V>
+__device__ __forceinline__ float dT_in(long long j, long long s, V v) {
+    return fmaf(-0.5f, v(j + s), 0.5f * v(j - s));
+}
+
+// The voxel is neither first nor last along any axis (the x = 0 and last-index
+// rules of the differences and of their transposes do not apply).
+__device__ __forceinline__ bool inner_voxel(const AdjVol &a, int x, int y, int z) {
+    return x >= 1 && x <= a.W - 2 && y >= 1 && y <= a.H - 2 && z >= 1 && z <= a.L - 2;
+}
+
 // delta(phi) with a fast division: the adjoint needs the derivative's value,
 // not the forward's bit pattern.
 __device__ __forceinline__ float dirac_fast(float phi, float eps) {
@@ -169,7 +184,8 @@ __device__ __forceinline__ float dirac_fast(float phi, float eps) {
 __device__ __forceinline__ long long nvox(const AdjVol &a) { return (long long)a.W * a.H * a.L; }
 __device__ __forceinline__ long long item(const BlockVol &bv) { return bv.t * kThreads + threadIdx.x; }
 
-__global__ void __launch_bounds__(kThreads) adj_heaviside(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_heaviside(AdjConst c, const AdjVol *__restrict__ vols,
+                                                          const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long i = item(bv);
@@ -178,7 +194,8 @@ __global__ void __launch_bounds__(kThreads) adj_heaviside(AdjConst c, const AdjV
 
 // Valid correlation along x of (I H, H, I (1-H), 1-H): (Wv, H, L) per field,
 // from H in phi2 to xs.
-__global__ void __launch_bounds__(kThreads) adj_blur_x(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blur_x(AdjConst c, const AdjVol *__restrict__ vols,
+                                                       const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long n = (long long)a.Wv * a.H * a.L;
@@ -231,7 +248,8 @@ constexpr int kNB = 8;   // outputs per thread along z
 constexpr int kNBy = 4;  // outputs per thread along y (shorter columns keep more threads in flight)
 
 // Valid correlation along y: xs (Wv, H, L) -> ys (Wv, Hv, L), four fields.
-__global__ void __launch_bounds__(kThreads) adj_blur_y(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blur_y(AdjConst c, const AdjVol *__restrict__ vols,
+                                                       const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long nin = (long long)a.Wv * a.H * a.L, n = (long long)a.Wv * a.Hv * a.L;
@@ -254,7 +272,8 @@ __global__ void __launch_bounds__(kThreads) adj_blur_y(AdjConst c, const AdjVol 
 // Valid correlation along z, then the data-term adjoint at each valid voxel:
 // writes (B1_bar - B3_bar, B2_bar - B4_bar) in the valid layout to xs and
 // e_out, e_in at the full-volume index to xs + 2N, xs + 3N.
-__global__ void __launch_bounds__(kThreads) adj_blur_z_data(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blur_z_data(AdjConst c, const AdjVol *__restrict__ vols,
+                                                            const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long N = nvox(a);
@@ -293,7 +312,8 @@ __global__ void __launch_bounds__(kThreads) adj_blur_z_data(AdjConst c, const Ad
 }
 
 // Transposed (full) correlation along z: xs (Wv, Hv, Lv) -> ys (Wv, Hv, L), two fields.
-__global__ void __launch_bounds__(kThreads) adj_blurT_z(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blurT_z(AdjConst c, const AdjVol *__restrict__ vols,
+                                                        const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long nin = (long long)a.Wv * a.Hv * a.Lv, n = (long long)a.Wv * a.Hv * a.L;
@@ -313,7 +333,8 @@ __global__ void __launch_bounds__(kThreads) adj_blurT_z(AdjConst c, const AdjVol
 }
 
 // Transposed correlation along y: ys (Wv, Hv, L) -> ys + 2N (Wv, H, L).
-__global__ void __launch_bounds__(kThreads) adj_blurT_y(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blurT_y(AdjConst c, const AdjVol *__restrict__ vols,
+                                                        const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long nin = (long long)a.Wv * a.Hv * a.L, n = (long long)a.Wv * a.H * a.L;
@@ -336,7 +357,8 @@ __global__ void __launch_bounds__(kThreads) adj_blurT_y(AdjConst c, const AdjVol
 
 // Transposed correlation along x and H_bar = I * P~ + Q~ over the volume,
 // into phi2 (0 for a volume without a valid region).
-__global__ void __launch_bounds__(kThreads) adj_blurT_x_hbar(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_blurT_x_hbar(AdjConst c, const AdjVol *__restrict__ vols,
+                                                             const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long N = nvox(a);
@@ -363,7 +385,8 @@ __global__ void __launch_bounds__(kThreads) adj_blurT_x_hbar(AdjConst c, const A
 // Gradient g = D phi and unit normals n = g / (|g| + 1e-6), stored so that
 // the stencil adjoint reads them at its neighbours instead of recomputing:
 // g_x, g_y to xs, xs + N; g_z, n_x, n_y, n_z to ys .. ys + 3N.
-__global__ void __launch_bounds__(kThreads) adj_normals(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kThreads) adj_normals(AdjConst c, const AdjVol *__restrict__ vols,
+                                                        const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long N = nvox(a);
@@ -374,8 +397,17 @@ __global__ void __launch_bounds__(kThreads) adj_normals(AdjConst c, const AdjVol
     const long long t1 = i / a.W;
     const int y = (int)(t1 % a.H);
     const int z = (int)(t1 / a.H);
-    const float gx = diff_x_at(g, a.phi, i, x), gy = diff_axis_at(a.phi, i, y, a.H, a.W),
-                gz = diff_axis_at(a.phi, i, z, a.L, (long long)a.W * a.H);
+    const long long plane = (long long)a.W * a.H;
+    float gx, gy, gz;
+    if (inner_voxel(a, x, y, z)) {
+        gx = 0.5f * (a.phi[i + 1] - a.phi[i - 1]);
+        gy = 0.5f * (a.phi[i + a.W] - a.phi[i - a.W]);
+        gz = 0.5f * (a.phi[i + plane] - a.phi[i - plane]);
+    } else {
+        gx = diff_x_at(g, a.phi, i, x);
+        gy = diff_axis_at(a.phi, i, y, a.H, a.W);
+        gz = diff_axis_at(a.phi, i, z, a.L, plane);
+    }
     const float rs = __frcp_rn(sqrtf(gx * gx + gy * gy + gz * gz) + 1e-6f);
     a.xs[i] = gx;
     a.xs[N + i] = gy;
@@ -404,7 +436,8 @@ __device__ __forceinline__ Col col_of(const AdjVol &a, long long t, int zdepth) 
 // block (the same four addresses for every block, so their number matters).
 // kappa_bar = u dt (nu delta - mu) is written over e_out (read first, by the
 // same thread) for adj_w.
-__global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
+__global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const AdjVol *__restrict__ vols,
+                                                       const int *__restrict__ pre,
                                                        double *grads) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
@@ -477,7 +510,8 @@ __global__ void __launch_bounds__(kBX * kBY) adj_point(AdjConst c, const AdjVol 
 // with n_bar = D^T kappa_bar, to be gathered by D_a^T.  kappa_bar comes from
 // adj_point; Lap_bar = u dt mu.  Each thread reads g and n at its own voxel
 // only, so w is written over g in place.
-__global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre) {
+__global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__restrict__ vols,
+                                                   const int *__restrict__ pre) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long N = nvox(a);
@@ -497,10 +531,22 @@ __global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__r
         const float mag = sqrtf(gx * gx + gy * gy + gz * gz);
         const float rs = __frcp_rn(mag + 1e-6f);
         const float inv_mag = mag > 0.0f ? __frcp_rn(mag) : 0.0f;
-        const float nbx = dT_x(g, i, x, N, kbar), nby = dT_axis(i, y, a.H, a.W, kbar),
-                    nbz = dT_axis(i, z, a.L, plane, kbar);
-        const float lbx = dT_x(g, i, x, N, lbar), lby = dT_axis(i, y, a.H, a.W, lbar),
-                    lbz = dT_axis(i, z, a.L, plane, lbar);
+        float nbx, nby, nbz, lbx, lby, lbz;
+        if (inner_voxel(a, x, y, z)) {
+            nbx = dT_in(i, 1, kbar);
+            nby = dT_in(i, a.W, kbar);
+            nbz = dT_in(i, plane, kbar);
+            lbx = dT_in(i, 1, lbar);
+            lby = dT_in(i, a.W, lbar);
+            lbz = dT_in(i, plane, lbar);
+        } else {
+            nbx = dT_x(g, i, x, N, kbar);
+            nby = dT_axis(i, y, a.H, a.W, kbar);
+            nbz = dT_axis(i, z, a.L, plane, kbar);
+            lbx = dT_x(g, i, x, N, lbar);
+            lby = dT_axis(i, y, a.H, a.W, lbar);
+            lbz = dT_axis(i, z, a.L, plane, lbar);
+        }
         const float ndot = nbx * nx[i] + nby * ny[i] + nbz * nz[i];
         gxa[i] = lbx + (nbx - ndot * gx * inv_mag) * rs;
         gya[i] = lby + (nby - ndot * gy * inv_mag) * rs;
@@ -509,8 +555,8 @@ __global__ void __launch_bounds__(kBX * kBY) adj_w(AdjConst c, const AdjVol *__r
 }
 
 // out += sum_a D_a^T w_a; a non-finite result sets kFlagAdjointNonFinite.
-__global__ void __launch_bounds__(kBX * kBY) adj_gather(AdjConst c, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
-                                                        unsigned *flag) {
+__global__ void __launch_bounds__(kBX * kBY) adj_gather(AdjConst c, const AdjVol *__restrict__ vols,
+                                                        const int *__restrict__ pre, unsigned *flag) {
     const BlockVol bv = block_vol(pre, c.nvol);
     const AdjVol a = vols[bv.v];
     const long long N = nvox(a);
@@ -525,7 +571,10 @@ __global__ void __launch_bounds__(kBX * kBY) adj_gather(AdjConst c, const AdjVol
     const int z1 = min(cl.z0 + kWZ, a.L);
     for (int z = cl.z0; z < z1 && x < a.W && y < a.H; ++z) {
         const long long i = ((long long)z * a.H + y) * a.W + x;
-        const float v = a.out[i] + (dT_x(g, i, x, N, vx) + dT_axis(i, y, a.H, a.W, vy) + dT_axis(i, z, a.L, plane, vz));
+        const float d = inner_voxel(a, x, y, z)
+                            ? dT_in(i, 1, vx) + dT_in(i, a.W, vy) + dT_in(i, plane, vz)
+                            : dT_x(g, i, x, N, vx) + dT_axis(i, y, a.H, a.W, vy) + dT_axis(i, z, a.L, plane, vz);
+        const float v = a.out[i] + d;
         a.out[i] = v;
         if (!isfinite(v) && flag) atomicOr(flag, kFlagAdjointNonFinite);
     }
@@ -559,7 +608,7 @@ void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]) {
     for (int j = 0; j < NADJ; j++) tiles[j] = t[j] > 0x7fffffffLL ? -1 : (int)t[j];
 }
 
-cudaError_t launch_step_adjoint(const float *taps, int k, const AdjScalars &s, const AdjVol *__restrict__ vols, const int *__restrict__ pre,
+cudaError_t launch_step_adjoint(const float *taps, int k, const AdjScalars &s, const AdjVol *vols, const int *pre,
                                 int n, const int *tot, double *grads, unsigned *flag, cudaStream_t st) {
     AdjConst c;
     for (int t = 0; t < MAXK; t++) c.taps[t] = t < k ? taps[t] : 0.0f;
