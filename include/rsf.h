@@ -146,7 +146,7 @@ size_t rsf_workspace_bytes_for(int64_t max_voxels, int32_t max_subvols);
 
 /* Kernel launch shapes for the workspace's later calls, overriding the
  * per-batch heuristics (0, or -1 for z_tma, restores them): x-pass outputs
- * per lane (5 or 9), stencil planes per block (32 or 64) and whether the
+ * per lane (5 or 9), stencil planes per block (32, 64 or 128) and whether the
  * 21/35-tap z-pass takes its planes through TMA (1) or the streaming ring
  * (0).  Results do not depend on the choice (every shape is bit-identical);
  * rsf_gb300.autotune.tune_launch_shape measures them on a batch.  No

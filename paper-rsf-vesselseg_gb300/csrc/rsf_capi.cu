@@ -295,8 +295,9 @@ rsf_status rsf_workspace_set_launch_shape(rsf_workspace *ws, int32_t xpass_width
     if (!ws) return fail(RSF_ERR_INVALID_ARGUMENT, "workspace is null");
     if (xpass_width != 0 && xpass_width != rsf::XB_CHOICES[0] && xpass_width != rsf::XB_CHOICES[1])
         return fail(RSF_ERR_INVALID_ARGUMENT, "x-pass width must be 0 (automatic), 5 or 9");
-    if (stencil_planes != 0 && stencil_planes != rsf::ST_ZC && stencil_planes != rsf::ST_ZC / 2)
-        return fail(RSF_ERR_INVALID_ARGUMENT, "stencil planes must be 0 (automatic), 32 or 64");
+    if (stencil_planes != 0 && stencil_planes != rsf::ST_ZC_MAX && stencil_planes != rsf::ST_ZC &&
+        stencil_planes != rsf::ST_ZC / 2)
+        return fail(RSF_ERR_INVALID_ARGUMENT, "stencil planes must be 0 (automatic), 32, 64 or 128");
     if (z_tma < -1 || z_tma > 1) return fail(RSF_ERR_INVALID_ARGUMENT, "z_tma must be -1 (automatic), 0 or 1");
     ws->force_xb = xpass_width;
     ws->force_zc = stencil_planes;

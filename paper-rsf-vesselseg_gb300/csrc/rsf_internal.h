@@ -20,7 +20,8 @@ constexpr int ZB_ZB = 16;      // generic z-pass: outputs per thread along z
 constexpr int ST_OX = 30;      // stencil: output columns per warp (lanes 1..30)
 constexpr int ST_OY = 14;      // stencil: output rows per block (warps 1..14)
 constexpr int ST_WARPS = ST_OY + 2;
-constexpr int ST_ZC = 64;      // stencil: planes per block (32 when that gives too few blocks)
+constexpr int ST_ZC = 64;      // stencil: planes per block (chosen per launch: 32, 64 or ST_ZC_MAX)
+constexpr int ST_ZC_MAX = 128;
 
 // The x-pass lane width (outputs per lane) is chosen per launch from these.
 constexpr int XB_CHOICES[2] = {5, 9};

@@ -806,7 +806,7 @@ __global__ void __launch_bounds__(ZB_TX) zpass_generic_kernel(const SubVolDev *_
 // ---------------------------------------------------------------------------
 // Stencil / update.  A block is ST_WARPS warps, one image row each (rows
 // y0-1 .. y0+ST_OY; the outer two are halo rows), 32 lanes wide (columns
-// x0-1 .. x0+30; lanes 0 and 31 are halo columns), streaming ST_ZC planes.
+// x0-1 .. x0+30; lanes 0 and 31 are halo columns), streaming c.zc planes.
 // Each step computes the gradient / normalised gradient of plane s+1 once
 // per thread, exchanges x neighbours by warp shuffles and y neighbours
 // through triple-buffered shared rows (one barrier per plane), and writes the

@@ -107,7 +107,7 @@ class Workspace:
 
     def set_launch_shape(self, xpass_width: int = 0, stencil_planes: int = 0, z_tma: int = -1):
         """Overrides the per-batch launch-shape heuristics for later calls:
-        x-pass outputs per lane (5 or 9), stencil planes per block (32 or 64)
+        x-pass outputs per lane (5 or 9), stencil planes per block (32, 64 or 128)
         and the TMA z-pass (1) or the streaming one (0); 0 / -1 restore the
         automatic choice.  Every shape gives bit-identical results."""
         check(self._lib.rsf_workspace_set_launch_shape(self.handle, int(xpass_width), int(stencil_planes),

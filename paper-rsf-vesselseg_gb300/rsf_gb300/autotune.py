@@ -121,12 +121,13 @@ def tune_cores(shape: Sequence[int], params: Params, halo: int = 32, dtype: str 
 # Kernel launch shapes.  The kernels take three shape choices per launch: the
 # x-pass lane width (5 or 9 outputs per lane: which wastes fewer outputs past
 # the valid width depends on the batch's row lengths), the stencil's planes
-# per block (64, or 32 for batches too small to fill the GPU several times)
+# per block (128 or 64, or 32 for batches too small to fill the GPU several
+# times)
 # and, for 21 and 35 taps, whether the z-pass takes its planes through TMA.
 # The workspace picks them by heuristics; `tune_launch_shape` times every
 # combination on the caller's batch and keeps the fastest.
 # ---------------------------------------------------------------------------
-LAUNCH_CANDIDATES = tuple((xb, zc, zt) for xb in (5, 9) for zc in (64, 32) for zt in (0, 1))
+LAUNCH_CANDIDATES = tuple((xb, zc, zt) for xb in (5, 9) for zc in (128, 64, 32) for zt in (0, 1))
 
 
 @dataclass

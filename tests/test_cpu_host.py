@@ -313,14 +313,14 @@ def test_plan_rejects_bounds_that_do_not_partition():
 def test_launch_shape_autotuner_picks_the_fastest():
     from rsf_gb300 import autotune
 
-    assert len(autotune.LAUNCH_CANDIDATES) == 8
-    assert len(set(autotune.LAUNCH_CANDIDATES)) == 8
+    assert len(autotune.LAUNCH_CANDIDATES) == 12
+    assert len(set(autotune.LAUNCH_CANDIDATES)) == 12
     times = {shape: 10.0 + i for i, shape in enumerate(autotune.LAUNCH_CANDIDATES)}
     fastest = autotune.LAUNCH_CANDIDATES[5]
     times[fastest] = 1.0
     best = autotune.pick_launch_shape(list(times.items()))
     assert (best.xpass_width, best.stencil_planes, best.z_tma) == fastest
-    assert best.ms_per_iteration == 1.0 and len(best.table) == 8
+    assert best.ms_per_iteration == 1.0 and len(best.table) == 12
 
 
 def test_launch_shape_override_rejects_bad_values_without_device(rsflib):
