@@ -283,7 +283,8 @@ struct Ring {
         if (act && i < n) {
             cp_async8(slot(i), src + (size_t)i * stride);
             if (sact && i >= first)
-                cp_async4(sslot(i), reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(sbyte(i)) & ~(uintptr_t)3));
+                cp_async4(sslot(i),
+                          reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(sbyte(i)) & ~(uintptr_t)3));
         }
     }
 };
