@@ -584,7 +584,7 @@ long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
 
 }  // namespace
 
-void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]) {
+void adjoint_tiles(const AdjVol &v, bool streamed, int tiles[NADJ]) {
     const long long N = (long long)v.W * v.H * v.L;
     const bool valid = v.Wv > 0;
     const long long bxy = cdiv(v.W, kBX) * cdiv(v.H, kBY);
@@ -599,7 +599,6 @@ void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]) {
         t[ADJ_TZ] = cdiv((long long)v.Wv * v.Hv * cdiv(v.L, kNB), kThreads);
         t[ADJ_TY] = cdiv((long long)v.Wv * cdiv(v.H, kNBy) * v.L, kThreads);
     }
-    (void)k;
     t[ADJ_TX] = cdiv(N, kThreads);
     t[ADJ_NRM] = cdiv(N, kThreads);
     t[ADJ_PT] = bxy * cdiv(v.L, kPointZ);

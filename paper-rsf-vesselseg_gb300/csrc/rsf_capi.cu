@@ -766,7 +766,7 @@ rsf_status rsf_step_adjoint_batched(rsf_workspace *ws, const rsf_params *p, rsf_
         rsf::valid_extents(a.W, a.H, a.L, k, a.Wv, a.Hv, a.Lv, wp);
         off += (size_t)(v.W * v.H * v.L);
         int tiles[rsf::NADJ];
-        rsf::adjoint_tiles(a, k, kspec > 0, tiles);
+        rsf::adjoint_tiles(a, kspec > 0, tiles);
         for (int j = 0; j < rsf::NADJ; j++) {
             const int64_t next = (int64_t)h_pre[j * n1 + i] + tiles[j];
             if (tiles[j] < 0 || next > 0x7fffffffLL) return fail(RSF_ERR_SHAPE, "batch needs more than 2^31 blocks");

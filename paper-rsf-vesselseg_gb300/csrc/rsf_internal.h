@@ -165,7 +165,7 @@ constexpr int NADJ = 11;
 enum AdjKernel { ADJ_H, ADJ_BX, ADJ_BY, ADJ_BZ, ADJ_TZ, ADJ_TY, ADJ_TX, ADJ_NRM, ADJ_PT, ADJ_W, ADJ_G };
 // Blocks of each adjoint kernel for one volume; with `streamed` the
 // recompute (ADJ_H .. ADJ_BZ) runs in the forward step's kernels instead.
-void adjoint_tiles(const AdjVol &v, int k, bool streamed, int tiles[NADJ]);
+void adjoint_tiles(const AdjVol &v, bool streamed, int tiles[NADJ]);
 
 #define RSF_DECLARE_K(K)                                                                                      \
     cudaError_t launch_xpass_##K(const SubVolDev *, const int *, int, const StepConst &, int, int, cudaStream_t); \

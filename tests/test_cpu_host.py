@@ -328,6 +328,18 @@ def test_launch_shape_override_rejects_bad_values_without_device(rsflib):
     assert rsflib.rsf_workspace_set_launch_shape(None, 0, 0, -1) == 1
 
 
+def test_batched_adjoint_rejects_bad_arguments_without_device(rsflib):
+    """rsf_step_adjoint_batched checks its workspace and table before any
+    device work: a null workspace or a null table is an invalid argument."""
+    from rsf_gb300._lib import RsfAdjointSubvol, RsfParams
+
+    p = RsfParams()
+    assert rsflib.rsf_params_default(ctypes.byref(p)) == 0
+    arr = (RsfAdjointSubvol * 1)()
+    assert rsflib.rsf_step_adjoint_batched(None, ctypes.byref(p), 0, arr, 1, None, None) == 1
+    assert "workspace" in rsflib.rsf_last_error().decode()
+
+
 def _gather_worker(rank, world, port, q):
     import os
 
